@@ -1,0 +1,15 @@
+"""fringe_gb300 -- GB300-native (sm_103a) phase linking for FRInGE stacks.
+
+The hot path of FRInGE's evd / phase_link modules (SHP gather, coherence
+matrix, EVD / MLE / STBAS eigen-solve, phase referencing, compressed SLC and
+temporal coherence) runs as CUDA kernels behind the C ABI declared in
+``include/fringe_gb300.h``.  Python entry points:
+
+* ``phase_link(stack, nmap, half_window, ...)`` -- in-memory run;
+* ``evdlib.Evd`` / ``phase_linklib.Phaselink`` -- drop-in replacements of the
+  reference's module wrappers (file level);
+* ``synth`` -- seeded synthetic stacks and SHP bitmasks.
+"""
+from .linker import phase_link  # noqa: F401
+
+__all__ = ["phase_link"]

@@ -1,0 +1,314 @@
+// api.cu -- C ABI of libfringe_gb300.so: contexts and in-memory runs.
+//
+// fpl_run replaces the OpenMP pixel loop of evd_process
+// (src/evd/evd.cpp:512-788; src/phase_link/phase_link.cpp:479-666) for a
+// scene held in memory.  The FP32 kernel handles every pixel; pixels whose
+// discrete decisions fall inside the FP32 rounding band are queued on the
+// device and settled by the FP64 kernel launched right behind it on the same
+// stream.  No host round trip separates the two passes.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/fringe_gb300.h"
+#include "ctx.h"
+#include "kernels.h"
+#include "pixel.cuh"
+
+using fpl::KParams;
+
+namespace {
+
+int cuda_fail(fpl_ctx *ctx, cudaError_t e, const char *what)
+{
+    if (ctx) {
+        ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    }
+    if (e == cudaErrorMemoryAllocation) return FPL_ERR_NOMEM;
+    return FPL_ERR_CUDA;
+}
+
+#define FPL_CUDA(ctx, call)                                             \
+    do {                                                                \
+        cudaError_t _e = (call);                                        \
+        if (_e != cudaSuccess) return cuda_fail((ctx), _e, #call);      \
+    } while (0)
+
+int grow(fpl_ctx *ctx, void **p, size_t *cap, size_t need)
+{
+    if (*cap >= need) return FPL_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(p, need);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc");
+    *cap = need;
+    return FPL_OK;
+}
+
+}  // namespace
+
+int fpl_validate_job(const fpl_job *job)
+{
+    if (!job) return FPL_ERR_NULL;
+    if (!job->stack || !job->nmap || !job->phase || !job->tcorr || !job->comp) return FPL_ERR_NULL;
+    if (job->rows <= 0 || job->cols <= 0 || job->nbands <= 0) return FPL_ERR_OPTIONS;
+    if (job->half_window_x < 0 || job->half_window_y < 0) return FPL_ERR_OPTIONS;
+    if (job->nbands > FPL_MAX_BANDS) return FPL_ERR_UNSUPPORTED;
+    const int K = (2 * job->half_window_y + 1) * (2 * job->half_window_x + 1);
+    if ((K + 31) / 32 > FPL_MAX_NULONG) return FPL_ERR_UNSUPPORTED;
+    if (job->method < FPL_METHOD_MLE || job->method > FPL_METHOD_STBAS) return FPL_ERR_OPTIONS;
+    if (job->semantics != FPL_SEM_EVD && job->semantics != FPL_SEM_PHASE_LINK) return FPL_ERR_OPTIONS;
+    if (job->mini_stack_count < 1 || job->mini_stack_count > job->nbands) return FPL_ERR_OPTIONS;
+    if (job->method == FPL_METHOD_STBAS) {
+        // src/evd/evd.cpp:74-91
+        if (job->band_width <= 0 || job->band_width >= job->nbands - 1) return FPL_ERR_OPTIONS;
+    }
+    if (job->precision != FPL_PREC_FP32 && job->precision != FPL_PREC_MIXED) return FPL_ERR_OPTIONS;
+    if (job->memory != FPL_MEM_HOST && job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
+    int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
+    if (r0 < 0 || r0 > r1 || r1 > job->rows) return FPL_ERR_OPTIONS;
+    return FPL_OK;
+}
+
+extern "C" {
+
+const char *fpl_version(void) { return "fringe_gb300 0.1 (sm_103a)"; }
+
+const char *fpl_error_string(int code)
+{
+    switch (code) {
+    case FPL_OK: return "ok";
+    case FPL_ERR_OPTIONS: return "invalid options";
+    case FPL_ERR_OPEN_STACK: return "cannot open the stack dataset";
+    case FPL_ERR_OPEN_WEIGHTS: return "cannot open the weights (nmap) dataset";
+    case FPL_ERR_WIDTH: return "width mismatch between stack and weights";
+    case FPL_ERR_LENGTH: return "length mismatch between stack and weights";
+    case FPL_ERR_NULONG: return "weights band count does not match the window";
+    case FPL_ERR_HALFWINDOWX: return "HALFWINDOWX of the weights differs from Nx";
+    case FPL_ERR_HALFWINDOWY: return "HALFWINDOWY of the weights differs from Ny";
+    case FPL_ERR_DATE: return "a stack band has no Date item in the slc metadata domain";
+    case FPL_ERR_OUT_EXISTS_DIR: return "output folder already exists";
+    case FPL_ERR_OUT_EXISTS_FILE: return "output folder path exists as a file";
+    case FPL_ERR_OUT_MKDIR: return "cannot create the output folder";
+    case FPL_ERR_CREATE_SLC: return "cannot create an output SLC";
+    case FPL_ERR_CREATE_AUX: return "cannot create tcorr / compressed SLC output";
+    case FPL_ERR_READ_STACK: return "error reading the stack";
+    case FPL_ERR_READ_WEIGHTS: return "error reading the weights";
+    case FPL_ERR_WRITE_SLC: return "error writing an output SLC";
+    case FPL_ERR_WRITE_AUX: return "error writing tcorr / compressed SLC";
+    case FPL_ERR_CUDA: return "CUDA runtime error";
+    case FPL_ERR_NOMEM: return "device memory allocation failed";
+    case FPL_ERR_UNSUPPORTED: return "unsupported size (nbands > 64 or window > 1024 taps)";
+    case FPL_ERR_DEVICE_CHECK: return "a kernel reported an internal error";
+    case FPL_ERR_NULL: return "a required pointer is NULL";
+    }
+    return "unknown error";
+}
+
+int fpl_ctx_create(int device, fpl_ctx **out)
+{
+    if (!out) return FPL_ERR_NULL;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
+    if (device < 0 || device >= ndev) return FPL_ERR_OPTIONS;
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+    fpl_ctx *ctx = new fpl_ctx();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete ctx; return cuda_fail(nullptr, e, "cudaStreamCreate"); }
+    cudaEventCreate(&ctx->ev0);
+    cudaEventCreate(&ctx->ev1);
+    e = cudaMalloc(&ctx->d_small, 256);
+    if (e != cudaSuccess) { fpl_ctx_destroy(ctx); return cuda_fail(nullptr, e, "cudaMalloc"); }
+    *out = ctx;
+    return FPL_OK;
+}
+
+int fpl_ctx_destroy(fpl_ctx *ctx)
+{
+    if (!ctx) return FPL_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    void *bufs[] = {ctx->d_stack, ctx->d_nmap, ctx->d_phase, ctx->d_tcorr, ctx->d_comp,
+                    ctx->d_status, ctx->d_fb_list, ctx->d_small};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return FPL_OK;
+}
+
+int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out)
+{
+    if (!ctx || !out) return FPL_ERR_NULL;
+    *out = ctx->stats;
+    return FPL_OK;
+}
+
+}  // extern "C"
+
+// Enqueues both passes on `st` for device buffers.  Scratch: the context's
+// work-list buffer (grown with cudaMalloc when too small) and d_small.
+int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
+                void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
+                bool fp64_all)
+{
+    const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
+    KParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.stack = static_cast<const float2 *>(stack);
+    P.nmap = nmap;
+    P.phase = static_cast<float2 *>(phase);
+    P.tcorr = tcorr;
+    P.comp = static_cast<float2 *>(comp);
+    P.status = status;
+    P.rows = job->rows;
+    P.cols = job->cols;
+    P.nb = job->nbands;
+    P.ny = job->half_window_y;
+    P.nx = job->half_window_x;
+    P.wx = 2 * job->half_window_x + 1;
+    P.K = (2 * job->half_window_y + 1) * P.wx;
+    P.nulong = (P.K + 31) / 32;
+    P.plane = (long long)job->rows * job->cols;
+    P.pix_begin = (long long)r0 * job->cols;
+    P.npix = (long long)(r1 - r0) * job->cols;
+    P.method = job->method;
+    P.semantics = job->semantics;
+    P.mini = job->mini_stack_count;
+    P.bw = job->band_width;
+    P.min_neigh = job->min_neighbors;
+    P.amb = ctx->amb_scale;
+    int *d_count = reinterpret_cast<int *>(ctx->d_small);
+    unsigned *d_err = reinterpret_cast<unsigned *>(static_cast<char *>(ctx->d_small) + 16);
+    P.fb_count = d_count;
+    P.err = d_err;
+    // work list: at most one entry per pixel of the range
+    size_t need = sizeof(long long) * (size_t)(P.npix > 0 ? P.npix : 1);
+    int rc = grow(ctx, &ctx->d_fb_list, &ctx->cap_fb_list, need);
+    if (rc) return rc;
+    P.fb_list = static_cast<long long *>(ctx->d_fb_list);
+    P.fb_cap = (int)(P.npix < 0x7fffffff ? P.npix : 0x7fffffff);
+    FPL_CUDA(ctx, cudaMemsetAsync(ctx->d_small, 0, 64, st));
+    if (P.npix == 0) return FPL_OK;
+    if (fp64_all) {
+        KParams Q = P;
+        Q.fb_list = nullptr;
+        FPL_CUDA(ctx, fpl::launch_fp64(Q, ctx->num_sms, st));
+        return FPL_OK;
+    }
+    FPL_CUDA(ctx, fpl::launch_fp32(P, ctx->num_sms, st));
+    FPL_CUDA(ctx, fpl::launch_fp64(P, ctx->num_sms, st));
+    return FPL_OK;
+}
+
+extern "C" {
+
+int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream)
+{
+    if (!ctx) return FPL_ERR_NULL;
+    int rc = fpl_validate_job(job);
+    if (rc) return rc;
+    if (job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
+    FPL_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    return fpl_enqueue(ctx, job, job->stack, job->nmap, job->phase, job->tcorr, job->comp,
+                       job->status, st, ctx->force_fp64);
+}
+
+int fpl_run(fpl_ctx *ctx, const fpl_job *job)
+{
+    if (!ctx) return FPL_ERR_NULL;
+    int rc = fpl_validate_job(job);
+    if (rc) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    FPL_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const size_t plane = (size_t)job->rows * job->cols;
+    const int nulong = ((2 * job->half_window_y + 1) * (2 * job->half_window_x + 1) + 31) / 32;
+    const size_t b_stack = plane * job->nbands * 8, b_nmap = plane * nulong * 4;
+    const size_t b_tc = plane * 4, b_comp = plane * 8, b_st = plane * 4;
+    const void *stack = job->stack;
+    const uint32_t *nmap = job->nmap;
+    void *phase = job->phase, *comp = job->comp;
+    float *tcorr = job->tcorr;
+    int32_t *status = job->status;
+    if (job->memory == FPL_MEM_HOST) {
+        if ((rc = grow(ctx, &ctx->d_stack, &ctx->cap_stack, b_stack))) return rc;
+        if ((rc = grow(ctx, &ctx->d_nmap, &ctx->cap_nmap, b_nmap))) return rc;
+        if ((rc = grow(ctx, &ctx->d_phase, &ctx->cap_phase, b_stack))) return rc;
+        if ((rc = grow(ctx, &ctx->d_tcorr, &ctx->cap_tcorr, b_tc))) return rc;
+        if ((rc = grow(ctx, &ctx->d_comp, &ctx->cap_comp, b_comp))) return rc;
+        if (job->status && (rc = grow(ctx, &ctx->d_status, &ctx->cap_status, b_st))) return rc;
+        FPL_CUDA(ctx, cudaMemcpyAsync(ctx->d_stack, job->stack, b_stack, cudaMemcpyHostToDevice, st));
+        FPL_CUDA(ctx, cudaMemcpyAsync(ctx->d_nmap, job->nmap, b_nmap, cudaMemcpyHostToDevice, st));
+        stack = ctx->d_stack;
+        nmap = static_cast<const uint32_t *>(ctx->d_nmap);
+        phase = ctx->d_phase;
+        tcorr = static_cast<float *>(ctx->d_tcorr);
+        comp = ctx->d_comp;
+        status = job->status ? static_cast<int32_t *>(ctx->d_status) : nullptr;
+    }
+    FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+    rc = fpl_enqueue(ctx, job, stack, nmap, phase, tcorr, comp, status, st, ctx->force_fp64);
+    if (rc) return rc;
+    FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+    if (job->memory == FPL_MEM_HOST) {
+        // rows outside [row_begin,row_end) are copied back as the device
+        // buffers hold them; only the computed rows are meaningful.
+        const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
+        const size_t off = (size_t)r0 * job->cols, cnt = (size_t)(r1 - r0) * job->cols;
+        for (int b = 0; b < job->nbands; ++b)
+            FPL_CUDA(ctx, cudaMemcpyAsync(static_cast<char *>(job->phase) + (b * plane + off) * 8,
+                                          static_cast<char *>(phase) + (b * plane + off) * 8, cnt * 8,
+                                          cudaMemcpyDeviceToHost, st));
+        FPL_CUDA(ctx, cudaMemcpyAsync(job->tcorr + off, tcorr + off, cnt * 4, cudaMemcpyDeviceToHost, st));
+        FPL_CUDA(ctx, cudaMemcpyAsync(static_cast<char *>(job->comp) + off * 8, static_cast<char *>(comp) + off * 8,
+                                      cnt * 8, cudaMemcpyDeviceToHost, st));
+        if (job->status)
+            FPL_CUDA(ctx, cudaMemcpyAsync(job->status + off, status + off, cnt * 4, cudaMemcpyDeviceToHost, st));
+    }
+    int small[8];
+    FPL_CUDA(ctx, cudaMemcpyAsync(small, ctx->d_small, sizeof(small), cudaMemcpyDeviceToHost, st));
+    FPL_CUDA(ctx, cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
+    ctx->stats.pixels = (long long)(r1 - r0) * job->cols;
+    ctx->stats.fp64_pixels = ctx->force_fp64 ? ctx->stats.pixels : small[0];
+    ctx->stats.mixed_fp64_inverse = 0;
+    ctx->stats.kernel_ms = ms;
+    ctx->stats.total_ms =
+        std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    unsigned err = static_cast<unsigned>(small[4]);
+    if (err) {
+        ctx->last_error = "device error flags " + std::to_string(err);
+        return FPL_ERR_DEVICE_CHECK;
+    }
+    return FPL_OK;
+}
+
+// test hooks: width of the FP32 ambiguity band, and FP64 for every pixel
+int fpl_ctx_set_tuning(fpl_ctx *ctx, float amb_scale, int force_fp64)
+{
+    if (!ctx) return FPL_ERR_NULL;
+    if (amb_scale >= 0.f) ctx->amb_scale = amb_scale;
+    ctx->force_fp64 = force_fp64 != 0;
+    return FPL_OK;
+}
+
+const char *fpl_ctx_last_error(const fpl_ctx *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+}  // extern "C"

@@ -1,0 +1,34 @@
+// ctx.h -- the library context behind the opaque fpl_ctx handle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/fringe_gb300.h"
+
+struct fpl_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // staging buffers for host-memory jobs (grown on demand)
+    void *d_stack = nullptr, *d_nmap = nullptr, *d_phase = nullptr, *d_tcorr = nullptr,
+         *d_comp = nullptr, *d_status = nullptr;
+    size_t cap_stack = 0, cap_nmap = 0, cap_phase = 0, cap_tcorr = 0, cap_comp = 0,
+           cap_status = 0;
+    // scratch: FP64 work list, and d_small = {count, .., err flags}
+    void *d_fb_list = nullptr;
+    size_t cap_fb_list = 0;
+    void *d_small = nullptr;
+    // tuning
+    float amb_scale = 8.0f;
+    bool force_fp64 = false;
+    fpl_stats stats = {};
+    std::string last_error;
+};
+
+int fpl_validate_job(const fpl_job *job);
+int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
+                void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
+                bool fp64_all);

@@ -1,0 +1,20 @@
+// kernels.h -- host-side declarations of the kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fpl {
+
+struct KParams;
+
+// padded order used for a stack depth (16, 32, 64; 0 = unsupported)
+int pick_np(int nb);
+
+// plain FP32 form over P.npix pixels starting at P.pix_begin
+cudaError_t launch_fp32(const KParams &P, int num_sms, cudaStream_t st);
+
+// FP64 form over the work list in P (or over every pixel if P.fb_list is null)
+cudaError_t launch_fp64(const KParams &P, int num_sms, cudaStream_t st);
+
+}  // namespace fpl

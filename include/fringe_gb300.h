@@ -1,0 +1,188 @@
+/*
+ * fringe_gb300.h -- C ABI of the GB300 phase-linking library
+ * (libfringe_gb300.so).
+ *
+ * The library replaces the per-pixel phase-linking loop of FRInGE's evd and
+ * phase_link modules with CUDA kernels for sm_103a.  Signatures use only
+ * plain C types and pointers; no C++ exceptions cross this boundary.
+ *
+ * Data layouts are the reference's in-memory layouts:
+ *   stack  complex64 (interleaved float re,im), band-planar [nbands][rows][cols]
+ *          -- src/evd/evd.cpp:195 (arma::cx_fmat cpxdata(cols*rows, nbands))
+ *   nmap   uint32 [rows][cols][nulong], nulong = ceil((2Ny+1)(2Nx+1)/32),
+ *          bit layout of include/fringe/ulongmask.hpp:55-94
+ *          -- src/evd/evd.cpp:197 (arma::Mat<uint> wts(nulong, pixels))
+ *   phase  complex64, band-planar [nbands][rows][cols] (evddata, evd.cpp:196)
+ *   tcorr  float32 [rows][cols]   (corr, evd.cpp:198)
+ *   comp   complex64 [rows][cols] (comp, evd.cpp:199)
+ *
+ * Return codes: 0 on success; the reference's module codes 101-121 where the
+ * same condition applies (src/evd/evd.cpp:54-121,157-165,213-261,278-355,
+ * 467-478,492-503,800-856); device-side failures use codes >= 200.
+ */
+#ifndef FRINGE_GB300_H
+#define FRINGE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- enums -------------------------------------------------------------- */
+enum fpl_method {            /* evdOptions::method, src/evd/evd.hpp:42 */
+    FPL_METHOD_MLE = 0,
+    FPL_METHOD_EVD = 1,
+    FPL_METHOD_STBAS = 2
+};
+
+enum fpl_semantics {         /* which reference module's loop is mirrored */
+    FPL_SEM_EVD = 0,         /* src/evd/evd.cpp:512-788         */
+    FPL_SEM_PHASE_LINK = 1   /* src/phase_link/phase_link.cpp:479-666 */
+};
+
+enum fpl_precision {
+    FPL_PREC_FP32 = 0,       /* plain FP32 form (FP64 only to settle ambiguous decisions) */
+    FPL_PREC_MIXED = 1       /* BF16 split-precision tensor-core coherence matrix */
+};
+
+enum fpl_memory {
+    FPL_MEM_HOST = 0,        /* pointers are host memory; the call stages them */
+    FPL_MEM_DEVICE = 1       /* pointers are device memory of the context's GPU */
+};
+
+/* per-pixel status values written to fpl_job::status (optional output) */
+enum fpl_pixel_status {
+    FPL_PX_OK = 0,
+    FPL_PX_SKIPPED_CENTRE = 1,    /* centre bit clear, evd.cpp:517 */
+    FPL_PX_TOO_FEW = 2,           /* npix < 2 / minNeighbors, evd.cpp:566 */
+    FPL_PX_EVD_FALLBACK = 3       /* phase_link: MLE not possible, EVD used */
+    /* negative values: the reference's tcorr codes -1 .. -7 */
+};
+
+/* return codes (device side; module codes 101-121 follow the reference) */
+#define FPL_OK                 0
+#define FPL_ERR_OPTIONS        101   /* bad options (evd.cpp:78-91 uses 101) */
+#define FPL_ERR_OPEN_STACK     102
+#define FPL_ERR_OPEN_WEIGHTS   105
+#define FPL_ERR_WIDTH          106
+#define FPL_ERR_LENGTH         107
+#define FPL_ERR_NULONG         108
+#define FPL_ERR_HALFWINDOWX    109
+#define FPL_ERR_HALFWINDOWY    110
+#define FPL_ERR_DATE           112
+#define FPL_ERR_OUT_EXISTS_DIR 113
+#define FPL_ERR_OUT_EXISTS_FILE 114
+#define FPL_ERR_OUT_MKDIR      115
+#define FPL_ERR_CREATE_SLC     116
+#define FPL_ERR_CREATE_AUX     117
+#define FPL_ERR_READ_STACK     118
+#define FPL_ERR_READ_WEIGHTS   119
+#define FPL_ERR_WRITE_SLC      120
+#define FPL_ERR_WRITE_AUX      121
+#define FPL_ERR_CUDA           201   /* a CUDA runtime call failed */
+#define FPL_ERR_NOMEM          202   /* device allocation failed */
+#define FPL_ERR_UNSUPPORTED    203   /* nbands > 64 or window > 1024 taps */
+#define FPL_ERR_DEVICE_CHECK   204   /* a kernel reported an internal error */
+#define FPL_ERR_NULL           205   /* a required pointer is NULL */
+
+#define FPL_MAX_BANDS 64
+#define FPL_MAX_NULONG 32
+
+typedef struct fpl_ctx fpl_ctx;
+
+/* ---- in-memory job -------------------------------------------------------
+ * One phase-linking pass over a scene held in memory: the body of the
+ * reference's per-block loop (src/evd/evd.cpp:512-788 and
+ * src/phase_link/phase_link.cpp:479-666) for every pixel of rows
+ * [row_begin, row_end) (row_end <= 0 means "to the last row").  Windows are
+ * clipped to the scene exactly as the reference's block logic makes them
+ * (evd.cpp:419-443,530-534), so results do not depend on blocking.        */
+typedef struct {
+    int rows, cols, nbands;
+    int half_window_y;       /* Ny (evdOptions::Ny)       */
+    int half_window_x;       /* Nx (evdOptions::Nx)       */
+    int method;              /* enum fpl_method           */
+    int semantics;           /* enum fpl_semantics        */
+    int mini_stack_count;    /* >= 1; reference date = mini_stack_count-1 */
+    int band_width;          /* STBAS bandwidth           */
+    int min_neighbors;       /* phase_link semantics only */
+    int precision;           /* enum fpl_precision        */
+    int memory;              /* enum fpl_memory           */
+    int row_begin, row_end;
+    const void *stack;       /* complex64 [nbands][rows][cols] */
+    const uint32_t *nmap;    /* [rows][cols][nulong]           */
+    void *phase;             /* complex64 [nbands][rows][cols] */
+    float *tcorr;            /* [rows][cols]                   */
+    void *comp;              /* complex64 [rows][cols]         */
+    int32_t *status;         /* optional [rows][cols]          */
+} fpl_job;
+
+/* statistics of the last fpl_run on a context */
+typedef struct {
+    long long pixels;            /* pixels in the row range          */
+    long long fp64_pixels;       /* pixels settled by the FP64 path  */
+    long long mixed_fp64_inverse;/* MLE pixels whose |G| inverse ran in FP64 */
+    float kernel_ms;             /* device time of the compute kernels */
+    float total_ms;              /* wall time of the call             */
+} fpl_stats;
+
+/* Creates a context on CUDA device `device` (owns a stream and scratch).
+ * Replaces the per-run set-up of evd_process (src/evd/evd.cpp:370-393). */
+int fpl_ctx_create(int device, fpl_ctx **out);
+int fpl_ctx_destroy(fpl_ctx *ctx);
+
+/* Synchronous in-memory run; host or device buffers per job->memory.
+ * Replaces the OpenMP pixel loop of evd_process
+ * (src/evd/evd.cpp:512-788; src/phase_link/phase_link.cpp:479-666). */
+int fpl_run(fpl_ctx *ctx, const fpl_job *job);
+
+/* Asynchronous run on `stream` (a cudaStream_t, NULL = the context's
+ * stream); device buffers only.  Same replacement as fpl_run. */
+int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream);
+
+int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out);
+
+/* ---- file-level module call ------------------------------------------------
+ * Mirrors evdOptions (src/evd/evd.hpp:19-54; src/phase_link/phase_link.hpp:20-57)
+ * and evd_process(evdOptions*) (src/evd/evd.cpp:16-888;
+ * src/phase_link/phase_link.cpp:17-755): reads a VRT / ENVI stack whose bands
+ * carry a "Date" item in metadata domain "slc", an ENVI nmap with
+ * HALFWINDOWX / HALFWINDOWY, and writes <date>.slc, tcorr.bin and the
+ * compressed SLC as ENVI BIP files.                                          */
+typedef struct {
+    const char *inputDS;                 /* stack VRT or ENVI file        */
+    const char *wtsDS;                   /* nmap ENVI file                */
+    const char *outputFolder;
+    const char *outputCompressedSlcFolder;   /* NULL: outputFolder   */
+    const char *compSlc;                 /* NULL: "compslc.bin"           */
+    int blocksize;                       /* default 64                    */
+    int memsize;                         /* MB, default 2048              */
+    int Nx, Ny;                          /* default 5, 5                  */
+    int minNeighbors;                    /* default 2                     */
+    int miniStackCount;                  /* default 1                     */
+    const char *method;                  /* "MLE" / "EVD" / "STBAS"       */
+    int bandWidth;                       /* default -1                    */
+    int semantics;                       /* enum fpl_semantics            */
+    int precision;                       /* enum fpl_precision            */
+    int device;                          /* CUDA device                   */
+    int verbose;                         /* print like the reference      */
+} fpl_options;
+
+/* Fills the defaults of evdOptions::evdOptions (src/evd/evd.hpp:58-68). */
+void fpl_options_default(fpl_options *opts);
+
+/* File-level run; returns 0 or the reference's module codes. */
+int fpl_process(const fpl_options *opts);
+
+/* Human-readable text for a return code. */
+const char *fpl_error_string(int code);
+
+/* Library version string. */
+const char *fpl_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

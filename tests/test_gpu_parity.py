@@ -1,0 +1,141 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Every case runs the same seeded inputs through libfringe_gb300.so and through
+the oracle's FP64 restatement of the reference loop, and checks validity codes
+(exact), wrapped phase RMS (<= 1e-3 rad), temporal coherence (<= 1e-4) and the
+exact zeros of skipped pixels.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from fringe_gb300 import synth
+from tests.parity import assert_parity, compare
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_both(stack, nmap, ny, nx, **kw):
+    from fringe_gb300 import phase_link
+    g = phase_link(stack, nmap, (ny, nx), want_status=True, **kw)
+    okw = {k: v for k, v in kw.items() if k in ("method", "semantics", "mini_stack_count",
+                                                  "band_width", "min_neighbors")}
+    o = oracle.run(stack, nmap, ny, nx, **okw)
+    return g, o
+
+
+@pytest.fixture(scope="module")
+def vor30():
+    return synth.scene("voronoi", 40, 72, 30, 5, 10, seed=1002)
+
+
+@pytest.mark.parametrize("method,semantics,extra", [
+    ("MLE", "evd", {}),
+    ("EVD", "evd", {}),
+    ("STBAS", "evd", {"band_width": 5}),
+    ("MLE", "phase_link", {"min_neighbors": 5}),
+    ("EVD", "phase_link", {}),
+    ("STBAS", "phase_link", {"band_width": 7}),
+    ("MLE", "evd", {"mini_stack_count": 4}),
+    ("EVD", "evd", {"mini_stack_count": 30}),
+])
+def test_voronoi_n30(gpu_lib, vor30, method, semantics, extra):
+    stack, nmap = vor30
+    g, o = _run_both(stack, nmap, 5, 10, method=method, semantics=semantics, **extra)
+    m = compare(g, o)
+    assert m["valid_both"] > 1000, m
+    assert_parity(m)
+
+
+@pytest.mark.parametrize("method", ["EVD", "MLE"])
+def test_uniform_n10(gpu_lib, method):
+    stack, nmap = synth.scene("uniform", 48, 48, 10, 5, 5, seed=1001)
+    g, o = _run_both(stack, nmap, 5, 5, method=method)
+    m = compare(g, o)
+    assert m["valid_both"] == 48 * 48, m
+    assert_parity(m)
+
+
+@pytest.mark.parametrize("nb", [1, 2, 3, 15, 16, 17, 31, 32, 33, 47, 63, 64])
+def test_depths(gpu_lib, nb):
+    stack, nmap = synth.scene("voronoi", 20, 24, nb, 2, 3, seed=100 + nb)
+    for method, sem in (("MLE", "evd"), ("EVD", "evd"), ("MLE", "phase_link")):
+        g, o = _run_both(stack, nmap, 2, 3, method=method, semantics=sem)
+        m = compare(g, o)
+        assert_parity(m)
+        if nb == 1:
+            both = (g["tcorr"] != 0) | np.isnan(g["tcorr"])
+            assert np.array_equal(np.isnan(g["tcorr"]), np.isnan(o["tcorr"]))
+
+
+def test_illconditioned_n64(gpu_lib):
+    stack, nmap = synth.scene("illcond", 24, 40, 64, 5, 10, seed=1003)
+    for method, sem in (("MLE", "evd"), ("MLE", "phase_link"), ("EVD", "evd")):
+        g, o = _run_both(stack, nmap, 5, 10, method=method, semantics=sem)
+        assert_parity(compare(g, o))
+
+
+def test_edge_masks_and_shapes(gpu_lib):
+    # empty nmap: every centre bit clear -> all outputs exactly zero
+    stack, nmap = synth.scene("uniform", 12, 15, 8, 2, 2, seed=5)
+    z = np.zeros_like(nmap)
+    g, o = _run_both(stack, z, 2, 2, method="MLE")
+    assert not np.any(g["phase"]) and not np.any(g["tcorr"]) and not np.any(g["comp"])
+    assert np.all(g["status"] == 1)
+    # centre bit only -> npix = 1 < 2 -> skipped
+    c = np.zeros_like(nmap)
+    flat = 2 * 5 + 2
+    c[..., flat // 32] = np.uint32(1 << (flat % 32))
+    g, o = _run_both(stack, c, 2, 2, method="EVD")
+    assert not np.any(g["phase"]) and np.all(g["status"] == 2)
+    # window larger than the scene, and a single row / column
+    for shape in ((3, 4), (1, 17), (19, 1), (1, 1)):
+        st, nm = synth.scene("uniform", shape[0], shape[1], 6, 5, 10, seed=9)
+        for method in ("MLE", "EVD"):
+            g, o = _run_both(st, nm, 5, 10, method=method)
+            assert_parity(compare(g, o))
+    # phase_link min_neighbors above the window size -> everything skipped
+    g, o = _run_both(stack, nmap, 2, 2, method="MLE", semantics="phase_link", min_neighbors=26)
+    assert not np.any(g["tcorr"]) and not np.any(o["tcorr"])
+
+
+def test_no_data_dates(gpu_lib):
+    """A date with zero power in a window gives 0/0 coherence; the defined
+    result is the failure code of the first eigen call (the reference's
+    LAPACK output is undefined there)."""
+    stack, nmap = synth.scene("uniform", 16, 16, 10, 2, 2, seed=5)
+    stack[3, :8, :8] = 0
+    stack[:, 12:, 12:] = 0
+    for method, sem in (("MLE", "evd"), ("EVD", "evd"), ("MLE", "phase_link")):
+        g, o = _run_both(stack, nmap, 2, 2, method=method, semantics=sem)
+        assert_parity(compare(g, o))
+
+
+def test_fp64_form_matches_oracle_tightly(gpu_lib, vor30):
+    from fringe_gb300 import _lib, phase_link
+    stack, nmap = vor30
+    ctx = _lib.Context(0)
+    ctx.set_tuning(force_fp64=True)
+    for method, sem in (("MLE", "evd"), ("EVD", "evd"), ("MLE", "phase_link")):
+        g = phase_link(stack, nmap, (5, 10), method=method, semantics=sem, ctx=ctx)
+        o = oracle.run(stack, nmap, 5, 10, method=method, semantics=sem)
+        m = compare(g, o)
+        assert_parity(m, phase_tol=1e-5, tcorr_tol=1e-5)
+    ctx.close()
+
+
+def test_row_range_and_torch_device_path(gpu_lib, vor30):
+    torch = pytest.importorskip("torch")
+    from fringe_gb300 import phase_link
+    stack, nmap = vor30
+    full = phase_link(stack, nmap, (5, 10), method="MLE")
+    part = phase_link(stack, nmap, (5, 10), method="MLE", rows=(10, 25))
+    assert np.array_equal(part["phase"][:, 10:25], full["phase"][:, 10:25])
+    assert np.array_equal(part["tcorr"][10:25], full["tcorr"][10:25])
+    ts = torch.from_numpy(stack).cuda()
+    tn = torch.from_numpy(nmap.view(np.int32)).cuda()
+    dev = phase_link(ts, tn, (5, 10), method="MLE")
+    torch.cuda.synchronize()
+    assert np.array_equal(dev["phase"].cpu().numpy(), full["phase"])
+    assert np.array_equal(dev["tcorr"].cpu().numpy(), full["tcorr"])
+    assert np.array_equal(dev["comp"].cpu().numpy(), full["comp"])
