@@ -1,0 +1,324 @@
+#!/usr/bin/env python3
+"""Benchmark: phase-linked pixels per second on one GB300 (or N replicas).
+
+Workload (the configuration the headline metric is quoted on): a synthetic
+2048 x 2048 scene, N = 30 dates, half-window 5 x 10 (11 x 21 = 231 taps),
+coherence gamma(dt) = 0.7 exp(-dt/24 d) + 0.2 on a 12-day grid, 8 amplitude
+classes on seeded Voronoi cells, nmap = same-class neighbours (SHP counts
+20..231), MLE with the reference evd semantics.  One step phase-links the
+whole scene.
+
+value : px/s with the stack and nmap resident in HBM (device pointers, no
+        copies in the timed region).  The 1 GB stack exceeds the 129 MB L2,
+        so no L2 flush is needed between steps.
+e2e   : px/s through the C ABI with pinned HOST buffers: every step copies the
+        stack + nmap to the device and phase + tcorr + compressed SLC back.
+roofline : the FP32 pixel kernel, timed with CUDA events on its stream.
+cpu_baseline : the oracle port (CPU restatement of the reference loop) on the
+        host cores, on a bounded row sample of the same scene.
+
+Under torchrun each rank phase-links its own scene (weak scaling, no
+data-path collective); value = all ranks' pixels / max-over-ranks time.
+``--impl reference`` times the reference's CPU implementation of the path
+(the oracle port; the reference's own LAPACK-linked build needs the reference
+tree) on rank 0 only.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NB, ROWS, COLS, NY, NX = 30, 2048, 2048, 5, 10
+SEED = 1002
+METRIC = "phase-linked px/s (N=30, 11x21)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--method", default="MLE", choices=["MLE", "EVD", "STBAS"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
+    ap.add_argument("--rows", type=int, default=ROWS)
+    ap.add_argument("--cols", type=int, default=COLS)
+    ap.add_argument("--cpu-rows", type=int, default=0,
+                    help="rows of the CPU-baseline sample (0 = auto)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def popcount_words(nmap):
+    cnt = np.zeros(nmap.shape[:2], np.int64)
+    for w in range(nmap.shape[2]):
+        v = nmap[..., w].astype(np.uint64)
+        c = v - ((v >> 1) & 0x55555555)
+        c = (c & 0x33333333) + ((c >> 2) & 0x33333333)
+        c = (((c + (c >> 4)) & 0x0F0F0F0F) * 0x01010101) >> 24
+        cnt += (c & 0xFF).astype(np.int64)
+    return cnt
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.idx = str(device_index)
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-i", self.idx, "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(stack, nmap, method, rows):
+    """Oracle port on the host cores over rows [0, rows) of the scene."""
+    import oracle
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.run(stack, nmap, NY, NX, method=method, rows=(0, rows), nthreads=threads)
+    dt = time.perf_counter() - t0
+    px = rows * stack.shape[2]
+    return {"value": px / dt, "unit": "px/s", "cores": threads, "kind": "port",
+            "sample": "rows 0..%d of the %dx%d scene (%d px), %s, evd semantics, %.1f s"
+                      % (rows, stack.shape[1], stack.shape[2], px, method, dt)}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from fringe_gb300 import synth
+    stack, nmap = synth.scene("voronoi", args.rows, args.cols, NB, NY, NX, seed=SEED)
+    import oracle
+    threads = os.cpu_count() or 1
+    rows = args.cpu_rows or 16
+    rows = min(rows, args.rows)
+    for _ in range(args.warmup):
+        oracle.run(stack, nmap, NY, NX, method=args.method, rows=(0, 2), nthreads=threads)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        r0 = (s * rows) % max(1, args.rows - rows)
+        oracle.run(stack, nmap, NY, NX, method=args.method, rows=(r0, r0 + rows), nthreads=threads)
+    dt = time.perf_counter() - t0
+    px = args.steps * rows * args.cols
+    v = px / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "px/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "voronoi %dx%d N=%d half-window %dx%d %s"
+                               % (args.rows, args.cols, NB, NY, NX, args.method),
+                   "sample_rows_per_step": rows},
+        "cpu_baseline": {"value": v, "unit": "px/s", "cores": threads, "kind": "port",
+                         "sample": "%d rows x %d cols per step" % (rows, args.cols)},
+        "e2e": {"value": v, "unit": "px/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from fringe_gb300 import _lib, build, phase_link, synth
+    build.build()
+    ctx = _lib.Context(local)
+
+    stack, nmap = synth.scene("voronoi", args.rows, args.cols, NB, NY, NX, seed=SEED + rank)
+    R, C = args.rows, args.cols
+    npx = R * C
+    shp = popcount_words(nmap)
+    sbar = float(shp.mean())
+
+    # ---- device-resident run (value) --------------------------------------
+    d_stack = torch.from_numpy(stack).cuda()
+    d_nmap = torch.from_numpy(nmap.view(np.int32)).cuda()
+    out = {"phase": torch.zeros((NB, R, C), dtype=torch.complex64, device="cuda"),
+           "tcorr": torch.zeros((R, C), dtype=torch.float32, device="cuda"),
+           "comp": torch.zeros((R, C), dtype=torch.complex64, device="cuda")}
+    kw = dict(method=args.method, precision=args.precision, ctx=ctx, out=out)
+    for _ in range(max(3, args.warmup)):
+        phase_link(d_stack, d_nmap, (NY, NX), **kw)
+    torch.cuda.synchronize()
+    fp64_px = None
+    ctx.set_profiling(True)
+    ctx.profile()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        phase_link(d_stack, d_nmap, (NY, NX), **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    k32_ms, k64_ms, runs = ctx.profile()
+    ctx.set_profiling(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * npx * args.steps / (ms / 1e3)
+    tc = out["tcorr"].cpu().numpy()
+    valid = int((tc > 0).sum())
+
+    # ---- end to end through the C ABI with pinned host buffers ---------------
+    e2e = None
+    if not args.no_e2e:
+        h_stack = torch.from_numpy(stack).pin_memory()
+        h_nmap = torch.from_numpy(nmap.view(np.int32)).pin_memory()
+        h_out = {"phase": torch.zeros((NB, R, C), dtype=torch.complex64).pin_memory(),
+                 "tcorr": torch.zeros((R, C), dtype=torch.float32).pin_memory(),
+                 "comp": torch.zeros((R, C), dtype=torch.complex64).pin_memory()}
+        np_out = {k: v.numpy() for k, v in h_out.items()}
+        hs, hn = h_stack.numpy(), h_nmap.numpy().view(np.uint32)
+        for _ in range(max(3, args.warmup)):
+            phase_link(hs, hn, (NY, NX), method=args.method, precision=args.precision,
+                       ctx=ctx, out=np_out)
+        st = ctx.stats()
+        fp64_px = st["fp64_pixels"]
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            phase_link(hs, hn, (NY, NX), method=args.method, precision=args.precision,
+                       ctx=ctx, out=np_out)
+        dt = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([dt], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        h2d = stack.nbytes + nmap.nbytes
+        d2h = sum(v.nbytes for v in np_out.values())
+        e2e = {"value": world * npx * args.steps / dt, "unit": "px/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+        assert np.array_equal(np_out["tcorr"], tc), "host and device paths differ"
+
+    if rank != 0:
+        return
+    hbm_peak, tf_peak, peak_src = load_peaks()
+    # dominant kernel: the FP32 pixel kernel, average launch duration
+    k_ms = k32_ms / max(runs, 1)
+    centre = shp > 0
+    flops = float((4.0 * NB * (NB + 1) * shp[centre]).sum())     # Gamma, Hermitian half
+    achieved_tf = flops / (k_ms / 1e3) / 1e12
+    alg_bytes = npx * (16 * NB + 4 * nmap.shape[2] + 12)
+    traffic = None
+    tf_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf_path):
+        with open(tf_path) as f:
+            tj = json.load(f)
+        if tj.get("kernel_bytes_per_px"):
+            traffic = tj["kernel_bytes_per_px"] * npx
+    line = {
+        "metric": METRIC, "value": value, "unit": "px/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "fp32" else "bf16x2-split/f32",
+        "data": "synthetic (seeded Voronoi scene, coherence model of tests/evd/test_evd.py)",
+        "config": {"workload": "voronoi %dx%d N=%d half-window %dx%d %s evd-semantics"
+                               % (R, C, NB, NY, NX, args.method),
+                   "precision": args.precision, "mean_shp": sbar,
+                   "l2": "inputs (1.0 GB stack) exceed L2; no flush needed",
+                   "valid_px": valid, "fp64_settled_px": fp64_px},
+        "e2e": e2e,
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+        "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": tf_peak,
+                     "unit": "TFLOP/s", "frac": achieved_tf / tf_peak, "traffic": traffic,
+                     "peak_source": peak_src,
+                     "kernel": "k_pixels<float> (FP32 SIMT Gamma + eigen-solves)",
+                     "kernel_ms": k_ms, "fp64_kernel_ms": k64_ms / max(runs, 1),
+                     "hbm_achieved_gbs": alg_bytes / (k_ms / 1e3) / 1e9,
+                     "hbm_peak_gbs": hbm_peak},
+    }
+    if not args.no_cpu:
+        rows = args.cpu_rows or 96
+        line["cpu_baseline"] = cpu_baseline(stack, nmap, args.method, min(rows, R))
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

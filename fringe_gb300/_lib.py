@@ -59,12 +59,14 @@ _SIGS = {
     "fpl_process": (ctypes.c_int, [ctypes.POINTER(FplOptions)]),
     "fpl_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "fpl_version": (ctypes.c_char_p, []),
-}
-# library extras (not part of the public header)
-_EXTRA = {
     "fpl_ctx_set_tuning": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
     "fpl_ctx_last_error": (ctypes.c_char_p, [_P]),
+    "fpl_ctx_set_profiling": (ctypes.c_int, [_P, ctypes.c_int]),
+    "fpl_ctx_profile": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_int)]),
 }
+_EXTRA = {}
 
 _lib = None
 _lock = threading.Lock()
@@ -138,6 +140,16 @@ class Context:
         s = FplStats()
         check(load().fpl_last_stats(self.handle, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in FplStats._fields_}
+
+    def set_profiling(self, on=True):
+        check(load().fpl_ctx_set_profiling(self.handle, int(on)), self.handle)
+
+    def profile(self):
+        """(fp32_ms, fp64_ms, runs) summed over runs since the last call."""
+        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        check(load().fpl_ctx_profile(self.handle, ctypes.byref(a), ctypes.byref(b),
+                                     ctypes.byref(n)), self.handle)
+        return a.value, b.value, n.value
 
     def set_tuning(self, amb_scale=-1.0, force_fp64=False):
         check(load().fpl_ctx_set_tuning(self.handle, float(amb_scale), int(force_fp64)), self.handle)

@@ -70,6 +70,7 @@ int fpl_validate_job(const fpl_job *job)
         if (job->band_width <= 0 || job->band_width >= job->nbands - 1) return FPL_ERR_OPTIONS;
     }
     if (job->precision != FPL_PREC_FP32 && job->precision != FPL_PREC_MIXED) return FPL_ERR_OPTIONS;
+    if (job->precision == FPL_PREC_MIXED) return FPL_ERR_UNSUPPORTED;   // tensor-core form not built yet
     if (job->memory != FPL_MEM_HOST && job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
     int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
     if (r0 < 0 || r0 > r1 || r1 > job->rows) return FPL_ERR_OPTIONS;
@@ -139,6 +140,7 @@ int fpl_ctx_destroy(fpl_ctx *ctx)
     if (!ctx) return FPL_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
     void *bufs[] = {ctx->d_stack, ctx->d_nmap, ctx->d_phase, ctx->d_tcorr, ctx->d_comp,
                     ctx->d_status, ctx->d_fb_list, ctx->d_small};
     for (void *b : bufs)
@@ -209,8 +211,20 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
         FPL_CUDA(ctx, fpl::launch_fp64(Q, ctx->num_sms, st));
         return FPL_OK;
     }
+    cudaEvent_t *ev = nullptr;
+    if (ctx->profile) {
+        while (ctx->prof_ev.size() < 3 * (ctx->prof_used + 1)) {
+            cudaEvent_t e;
+            FPL_CUDA(ctx, cudaEventCreate(&e));
+            ctx->prof_ev.push_back(e);
+        }
+        ev = &ctx->prof_ev[3 * ctx->prof_used++];
+        FPL_CUDA(ctx, cudaEventRecord(ev[0], st));
+    }
     FPL_CUDA(ctx, fpl::launch_fp32(P, ctx->num_sms, st));
+    if (ev) FPL_CUDA(ctx, cudaEventRecord(ev[1], st));
     FPL_CUDA(ctx, fpl::launch_fp64(P, ctx->num_sms, st));
+    if (ev) FPL_CUDA(ctx, cudaEventRecord(ev[2], st));
     return FPL_OK;
 }
 
@@ -223,7 +237,8 @@ int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream)
     if (rc) return rc;
     if (job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
     FPL_CUDA(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    // the stream is used as given: NULL is the legacy default stream
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     return fpl_enqueue(ctx, job, job->stack, job->nmap, job->phase, job->tcorr, job->comp,
                        job->status, st, ctx->force_fp64);
 }
@@ -310,5 +325,33 @@ int fpl_ctx_set_tuning(fpl_ctx *ctx, float amb_scale, int force_fp64)
 }
 
 const char *fpl_ctx_last_error(const fpl_ctx *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int fpl_ctx_set_profiling(fpl_ctx *ctx, int on)
+{
+    if (!ctx) return FPL_ERR_NULL;
+    ctx->profile = on != 0;
+    ctx->prof_used = 0;
+    return FPL_OK;
+}
+
+int fpl_ctx_profile(fpl_ctx *ctx, double *fp32_ms, double *fp64_ms, int *runs)
+{
+    if (!ctx) return FPL_ERR_NULL;
+    double a = 0.0, b = 0.0;
+    for (size_t r = 0; r < ctx->prof_used; ++r) {
+        cudaEvent_t *ev = &ctx->prof_ev[3 * r];
+        FPL_CUDA(ctx, cudaEventSynchronize(ev[2]));
+        float x = 0.f, y = 0.f;
+        FPL_CUDA(ctx, cudaEventElapsedTime(&x, ev[0], ev[1]));
+        FPL_CUDA(ctx, cudaEventElapsedTime(&y, ev[1], ev[2]));
+        a += x;
+        b += y;
+    }
+    if (fp32_ms) *fp32_ms = a;
+    if (fp64_ms) *fp64_ms = b;
+    if (runs) *runs = (int)ctx->prof_used;
+    ctx->prof_used = 0;
+    return FPL_OK;
+}
 
 }  // extern "C"

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/fringe_gb300.h"
 
@@ -24,6 +25,10 @@ struct fpl_ctx {
     // tuning
     float amb_scale = 8.0f;
     bool force_fp64 = false;
+    // optional per-kernel timing: one event triple per enqueued run
+    bool profile = false;
+    std::vector<cudaEvent_t> prof_ev;   // 3 per run: before FP32, between, after FP64
+    size_t prof_used = 0;
     fpl_stats stats = {};
     std::string last_error;
 };

@@ -138,11 +138,25 @@ int fpl_ctx_destroy(fpl_ctx *ctx);
  * (src/evd/evd.cpp:512-788; src/phase_link/phase_link.cpp:479-666). */
 int fpl_run(fpl_ctx *ctx, const fpl_job *job);
 
-/* Asynchronous run on `stream` (a cudaStream_t, NULL = the context's
- * stream); device buffers only.  Same replacement as fpl_run. */
+/* Asynchronous run on `stream` (a cudaStream_t used as given: NULL is the
+ * legacy default stream); device buffers only.  Runs sharing one context
+ * share its scratch, so they must not overlap on the GPU.  Same replacement
+ * as fpl_run. */
 int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream);
 
 int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out);
+
+/* ---- diagnostics (no counterpart in the reference) ------------------------ */
+/* Text of the last CUDA / device error seen by the context. */
+const char *fpl_ctx_last_error(const fpl_ctx *ctx);
+/* Tuning hooks: width of the FP32 rounding band (in units of n*eps*|A|_F,
+ * < 0 keeps the current value) and FP64 for every pixel (test use). */
+int fpl_ctx_set_tuning(fpl_ctx *ctx, float amb_scale, int force_fp64);
+/* Per-kernel device timing of subsequent runs (CUDA events on the run's
+ * stream); fpl_ctx_profile waits for them, returns the summed FP32 and FP64
+ * kernel milliseconds and the run count, and resets the record. */
+int fpl_ctx_set_profiling(fpl_ctx *ctx, int on);
+int fpl_ctx_profile(fpl_ctx *ctx, double *fp32_ms, double *fp64_ms, int *runs);
 
 /* ---- file-level module call ------------------------------------------------
  * Mirrors evdOptions (src/evd/evd.hpp:19-54; src/phase_link/phase_link.hpp:20-57)
