@@ -31,7 +31,7 @@ class FplJob(ctypes.Structure):
 
 class FplStats(ctypes.Structure):
     _fields_ = [("pixels", ctypes.c_longlong), ("fp64_pixels", ctypes.c_longlong),
-                ("mixed_fp64_inverse", ctypes.c_longlong),
+                ("mixed_fp64_inverse", ctypes.c_longlong), ("slow_path_pixels", ctypes.c_longlong),
                 ("kernel_ms", ctypes.c_float), ("total_ms", ctypes.c_float)]
 
 

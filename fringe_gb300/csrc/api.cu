@@ -15,7 +15,7 @@
 #include <mutex>
 #include <string>
 
-#include "../../include/fringe_gb300.h"
+#include "fringe_gb300.h"
 #include "ctx.h"
 #include "kernels.h"
 #include "pixel.cuh"
@@ -193,10 +193,12 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
     P.bw = job->band_width;
     P.min_neigh = job->min_neighbors;
     P.amb = ctx->amb_scale;
+    P.cond_max = ctx->cond_max;
     int *d_count = reinterpret_cast<int *>(ctx->d_small);
     unsigned *d_err = reinterpret_cast<unsigned *>(static_cast<char *>(ctx->d_small) + 16);
     P.fb_count = d_count;
     P.err = d_err;
+    P.slow = reinterpret_cast<int *>(static_cast<char *>(ctx->d_small) + 32);
     // work list: at most one entry per pixel of the range
     size_t need = sizeof(long long) * (size_t)(P.npix > 0 ? P.npix : 1);
     int rc = grow(ctx, &ctx->d_fb_list, &ctx->cap_fb_list, need);
@@ -295,7 +297,7 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job)
         if (job->status)
             FPL_CUDA(ctx, cudaMemcpyAsync(job->status + off, status + off, cnt * 4, cudaMemcpyDeviceToHost, st));
     }
-    int small[8];
+    int small[16];
     FPL_CUDA(ctx, cudaMemcpyAsync(small, ctx->d_small, sizeof(small), cudaMemcpyDeviceToHost, st));
     FPL_CUDA(ctx, cudaStreamSynchronize(st));
     float ms = 0.f;
@@ -304,6 +306,7 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job)
     ctx->stats.pixels = (long long)(r1 - r0) * job->cols;
     ctx->stats.fp64_pixels = ctx->force_fp64 ? ctx->stats.pixels : small[0];
     ctx->stats.mixed_fp64_inverse = 0;
+    ctx->stats.slow_path_pixels = small[8];
     ctx->stats.kernel_ms = ms;
     ctx->stats.total_ms =
         std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();

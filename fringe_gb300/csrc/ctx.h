@@ -6,7 +6,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/fringe_gb300.h"
+#include "fringe_gb300.h"
 
 struct fpl_ctx {
     int device = 0;
@@ -24,6 +24,7 @@ struct fpl_ctx {
     void *d_small = nullptr;
     // tuning
     float amb_scale = 8.0f;
+    float cond_max = 1000.0f;   // |C| inverted in FP32 up to this inf-norm condition
     bool force_fp64 = false;
     // optional per-kernel timing: one event triple per enqueued run
     bool profile = false;

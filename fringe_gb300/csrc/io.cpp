@@ -1,7 +1,7 @@
 // io.cpp -- file-level module call (fpl_process), mirroring evd_process.
 #include <cstring>
 
-#include "../../include/fringe_gb300.h"
+#include "fringe_gb300.h"
 
 extern "C" {
 

@@ -7,17 +7,20 @@
 //   1. SHP gather: the window is walked 32 taps at a time; the nmap bits of a
 //      tap chunk are compacted with a warp ballot and the selected samples
 //      (all dates) are staged in shared memory;
-//   2. Gamma = sum x x^H over the SHPs, register-blocked (each lane owns an
+//   2. Gamma = sum x x^H over the SHPs, register-blocked (each lane owns a
 //      BR x 4 block of the upper triangle), then normalised to coherence;
-//   3. eigen-solves in shared memory: Householder tridiagonalisation, warp
-//      multisection on the Sturm count, inverse iteration on the tridiagonal,
-//      back-transformation; Cholesky tests and inverse for MLE;
+//   3. eigen-solves in shared memory: power iteration for the EVD largest
+//      eigenvector (Householder path when it converges slowly); for MLE a
+//      Cholesky test of C, a symmetric-sweep inverse of |C|, then Householder
+//      tridiagonalisation, warp multisection on the Sturm count, inverse
+//      iteration on the tridiagonal and back-transformation;
 //   4. phase referencing, compressed SLC and temporal coherence with warp
 //      shuffles.
 // T = float is the plain FP32 form.  Discrete decisions (eigenvalue < 1e-6,
 // "is |Gamma| positive definite") whose FP32 answer lies inside a rounding
-// band are not taken in FP32: the pixel is appended to a list and settled by
-// the same code instantiated with T = double.
+// band, and |Gamma| whose condition estimate is too large for an FP32
+// inverse, are not settled in FP32: the pixel is appended to a list and
+// recomputed by the same code instantiated with T = double.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -39,11 +42,13 @@ struct KParams {
     long long pix_begin, npix;          // first pixel, pixel count
     int rows, cols, nb, ny, nx, wx, K, nulong;
     int method, semantics, mini, bw, min_neigh;
-    float amb;                          // width of the FP32 ambiguity band, in units of n*eps*|A|_F
+    float amb;                          // width of the FP32 rounding band, in units of n*eps*|A|_F
+    float cond_max;                     // largest inf-norm condition of |C| inverted in FP32
     int *fb_count;                      // FP64 work list (scratch)
     long long *fb_list;
     int fb_cap;
     unsigned *err;                      // error flags (scratch)
+    int *slow;                          // pixels that left the fast eigen path (scratch)
 };
 
 enum { M_MLE = 0, M_EVD = 1, M_STBAS = 2 };
@@ -71,6 +76,12 @@ template <typename T> __device__ __forceinline__ C2<T> cdiv(C2<T> a, C2<T> b)
     T den = b.x * b.x + b.y * b.y;
     return cmk<T>((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
 }
+// acc += a * b, acc -= a * b
+template <typename T> __device__ __forceinline__ void cfma(C2<T> &acc, C2<T> a, C2<T> b)
+{
+    acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
+    acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+}
 
 template <typename T> __device__ __forceinline__ T warp_sum(T v)
 {
@@ -95,6 +106,12 @@ template <typename T> struct Eps;
 template <> struct Eps<float> { static constexpr float v = 1.1920929e-7f; static constexpr float tiny = 1.17549435e-38f; };
 template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; static constexpr double tiny = 2.2250738585072014e-308; };
 
+// fast division where only a rounding-level result is needed (Sturm counts)
+__device__ __forceinline__ float fdiv_fast(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fdiv_fast(double a, double b) { return a / b; }
+__device__ __forceinline__ float rsqrt_t(float a) { return rsqrtf(a); }
+__device__ __forceinline__ double rsqrt_t(double a) { return rsqrt(a); }
+
 // ------------------------------------------------------------------------
 // per-warp shared-memory slab layout
 // ------------------------------------------------------------------------
@@ -104,42 +121,68 @@ __host__ __device__ constexpr size_t cmax(size_t a, size_t b) { return a > b ? a
 template <typename T, int NP> struct Lay {
     static constexpr int LD = NP + 1;        // matrix row stride (odd: conflict-free columns)
     static constexpr int XS = NP + 2;        // staging row stride in float2 (16-byte rows)
-    static constexpr size_t cm = 0;                                              // coherence C
-    static constexpr size_t wm = align16(cm + sizeof(C2<T>) * NP * LD);          // work matrix / staging
-    static constexpr size_t lr = align16(wm + cmax(sizeof(C2<T>) * NP * LD, sizeof(float2) * 32 * XS));
-    static constexpr size_t xr = align16(lr + sizeof(T) * NP * LD);              // real work 2
-    static constexpr size_t vw = align16(xr + sizeof(T) * NP * LD);              // complex vec w
-    static constexpr size_t tu = align16(vw + sizeof(C2<T>) * NP);               // tau
-    static constexpr size_t dd = align16(tu + sizeof(C2<T>) * NP);               // d
-    static constexpr size_t ee = align16(dd + sizeof(T) * NP);                   // e
-    static constexpr size_t e2 = align16(ee + sizeof(T) * NP);                   // e^2
-    static constexpr size_t yy = align16(e2 + sizeof(T) * NP);                   // y / misc real vec
-    static constexpr size_t ph = align16(yy + sizeof(T) * NP);                   // phases (float2)
+    static constexpr size_t mat = sizeof(C2<T>) * NP * LD;
+    static constexpr size_t cm = 0;                                   // coherence C
+    static constexpr size_t wm = align16(cm + mat);                   // work: staging / Cholesky / M / tridiag
+    static constexpr size_t wm_bytes = align16(cmax(mat, sizeof(float2) * 32 * XS));
+    static constexpr size_t xr = wm + align16(mat / 2);               // real sweep matrix: upper half of wm
+    static constexpr size_t vv = wm + wm_bytes;                       // complex vector v
+    static constexpr size_t ww = align16(vv + sizeof(C2<T>) * NP);    // complex vector w
+    static constexpr size_t tu = align16(ww + sizeof(C2<T>) * NP);    // tau
+    static constexpr size_t dd = align16(tu + sizeof(C2<T>) * NP);    // d
+    static constexpr size_t ee = align16(dd + sizeof(T) * NP);        // e
+    static constexpr size_t e2 = align16(ee + sizeof(T) * NP);        // e^2
+    static constexpr size_t yy = align16(e2 + sizeof(T) * NP);        // y / row k / 1/sqrt(P)
+    static constexpr size_t wk = align16(yy + sizeof(T) * NP);        // 5*NP scratch (lane 0)
+    static constexpr size_t ph = align16(wk + sizeof(T) * 5 * NP);    // phases (float2)
     static constexpr size_t bytes = align16(ph + sizeof(float2) * NP);
 };
 
 // ------------------------------------------------------------------------
-// warp Cholesky (lower, in place).  Returns false at the first pivot that is
-// not > 0 (or NaN), like zpotrf's test (AJJ <= 0 .or. disnan(AJJ)).
-// Keeps L in the lower triangle, sqrt pivots on the diagonal.
+// warp Cholesky (lower, in place) of the complex Hermitian matrix in A:
+// returns false at the first pivot that is not > 0 (or NaN), like zpotrf's
+// test (AJJ <= 0 .or. disnan(AJJ)).  col: NP complex smem scratch.
+// STORE: keep L in the lower triangle with 1 / L_jj on the diagonal (for the
+// triangular solves); otherwise only the Schur complements are updated.
 // ------------------------------------------------------------------------
-template <typename T, int LD>
-__device__ bool warp_chol_c(C2<T> *A, int n, int lane)
+template <typename T, int LD, int NP, bool STORE = false>
+__device__ bool warp_chol_c(C2<T> *A, int n, C2<T> *col, int lane)
 {
     for (int j = 0; j < n; ++j) {
-        T piv = A[j * LD + j].x;
+        const T piv = A[j * LD + j].x;
         if (!(piv > T(0))) return false;
-        T sq = sqrt(piv);
-        T r = T(1) / sq;
-        __syncwarp();
-        for (int i = j + 1 + lane; i < n; i += 32) A[i * LD + j] = cscale(A[i * LD + j], r);
-        if (lane == 0) A[j * LD + j] = cmk<T>(sq, T(0));
+        const T r = rsqrt_t(piv);
+        // scaled column j (l_k, k > j) into col[] for broadcast reads; zeros elsewhere
+        for (int k = lane; k < NP; k += 32) {
+            C2<T> l = (k > j && k < n) ? cscale(A[k * LD + j], r) : cmk<T>(T(0), T(0));
+            col[k] = l;
+            if (STORE && k > j && k < n) A[k * LD + j] = l;
+        }
+        if (STORE && lane == 0) A[j * LD + j] = cmk<T>(r, T(0));
         __syncwarp();
         for (int i = j + 1 + lane; i < n; i += 32) {
-            C2<T> li = A[i * LD + j];
-            for (int k = j + 1; k <= i; ++k) {
-                C2<T> lk = A[k * LD + j];
-                A[i * LD + k] = csub(A[i * LD + k], cmulc(li, lk));
+            const C2<T> li = col[i];
+            C2<T> *__restrict__ Ai = A + i * LD;
+            // A[i][k] -= l_i conj(l_k), k in (j, i]; col[k] = 0 for k <= j
+            const int k0 = (j + 1) & ~1;
+#pragma unroll 2
+            for (int k = k0; k <= i; k += 2) {
+                C2<T> l0, l1;
+                if (sizeof(T) == 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(col + k);
+                    l0 = cmk<T>(T(v.x), T(v.y));
+                    l1 = cmk<T>(T(v.z), T(v.w));
+                } else {
+                    l0 = col[k];
+                    l1 = col[k + 1];
+                }
+                C2<T> a0 = Ai[k], a1 = Ai[k + 1];
+                a0.x -= li.x * l0.x + li.y * l0.y;
+                a0.y -= li.y * l0.x - li.x * l0.y;
+                a1.x -= li.x * l1.x + li.y * l1.y;
+                a1.y -= li.y * l1.x - li.x * l1.y;
+                if (k > j) Ai[k] = a0;
+                if (k + 1 <= i) Ai[k + 1] = a1;
             }
         }
         __syncwarp();
@@ -147,31 +190,43 @@ __device__ bool warp_chol_c(C2<T> *A, int n, int lane)
     return true;
 }
 
-template <typename T, int LD>
-__device__ bool warp_chol_r(T *A, int n, int lane)
+// Solves (L L^H) x = b with the factor of warp_chol_c<STORE> (1/L_jj on the
+// diagonal).  b / x are lane-distributed (element i on lane i%32, slot i/32).
+template <typename T, int LD, int NP>
+__device__ void warp_chol_solve(const C2<T> *L, int n, C2<T> &b0, C2<T> &b1, int lane)
 {
+    const int i0 = lane, i1 = lane + 32;
+    // forward: L y = b
     for (int j = 0; j < n; ++j) {
-        T piv = A[j * LD + j];
-        if (!(piv > T(0))) return false;
-        T sq = sqrt(piv);
-        T r = T(1) / sq;
-        __syncwarp();
-        for (int i = j + 1 + lane; i < n; i += 32) A[i * LD + j] *= r;
-        if (lane == 0) A[j * LD + j] = sq;
-        __syncwarp();
-        for (int i = j + 1 + lane; i < n; i += 32) {
-            T li = A[i * LD + j];
-            for (int k = j + 1; k <= i; ++k) A[i * LD + k] -= li * A[k * LD + j];
-        }
-        __syncwarp();
+        const C2<T> own = (j < 32) ? b0 : b1;
+        C2<T> y;
+        y.x = __shfl_sync(0xffffffffu, own.x, j & 31);
+        y.y = __shfl_sync(0xffffffffu, own.y, j & 31);
+        y = cscale(y, L[j * LD + j].x);
+        if (i0 == j) b0 = y;
+        if (NP > 32 && i1 == j) b1 = y;
+        if (i0 > j && i0 < n) b0 = csub(b0, cmul(L[i0 * LD + j], y));
+        if (NP > 32 && i1 > j && i1 < n) b1 = csub(b1, cmul(L[i1 * LD + j], y));
     }
-    return true;
+    // backward: L^H x = y
+    for (int j = n - 1; j >= 0; --j) {
+        const C2<T> own = (j < 32) ? b0 : b1;
+        C2<T> x;
+        x.x = __shfl_sync(0xffffffffu, own.x, j & 31);
+        x.y = __shfl_sync(0xffffffffu, own.y, j & 31);
+        x = cscale(x, L[j * LD + j].x);
+        if (i0 == j) b0 = x;
+        if (NP > 32 && i1 == j) b1 = x;
+        // b_i -= conj(L_ji) x_j for i < j
+        if (i0 < j) b0 = csub(b0, ccmul(L[j * LD + i0], x));
+        if (NP > 32 && i1 < j) b1 = csub(b1, ccmul(L[j * LD + i1], x));
+    }
 }
 
-// lambda_min(A) vs thr: +1 certainly above, -1 certainly at or below,
-// 0 inside the rounding band [thr - delta, thr + delta].
-template <typename T, int LD>
-__device__ int lam_min_test_c(const C2<T> *A, C2<T> *W, int n, T thr, T delta, int lane)
+// lambda_min(A) vs thr for a complex Hermitian A (lower triangle read):
+// +1 certainly above, -1 certainly at or below, 0 inside [thr-delta, thr+delta].
+template <typename T, int LD, int NP>
+__device__ int lam_min_test_c(const C2<T> *A, C2<T> *W, C2<T> *col, int n, T thr, T delta, int lane)
 {
     const int nsh = delta > T(0) ? 2 : 1;
     for (int s = 0; s < nsh; ++s) {
@@ -182,7 +237,7 @@ __device__ int lam_min_test_c(const C2<T> *A, C2<T> *W, int n, T thr, T delta, i
             W[i * LD + i].x -= sh;
         }
         __syncwarp();
-        bool ok = warp_chol_c<T, LD>(W, n, lane);
+        bool ok = warp_chol_c<T, LD, NP>(W, n, col, lane);
         __syncwarp();
         if (nsh == 1) return ok ? 1 : -1;
         if (s == 0 && ok) return 1;
@@ -191,65 +246,79 @@ __device__ int lam_min_test_c(const C2<T> *A, C2<T> *W, int n, T thr, T delta, i
     return 0;
 }
 
-template <typename T, int LD>
-__device__ int lam_min_test_r(const T *A, T *W, int n, T thr, T delta, int lane)
+// ------------------------------------------------------------------------
+// symmetric sweep (Gauss-Jordan) inverse of a real symmetric matrix, in
+// place: sweeping every index leaves -inv(A).  The sweep pivots are the
+// LDL^T pivots, so "a pivot <= 0" is the same decision as a failing
+// Cholesky factorisation.  Lane i owns row i; all lanes work every step.
+// rowk: NP real smem scratch.  On success A holds inv(A) and *inf_norm the
+// largest absolute row sum of the inverse.
+// ------------------------------------------------------------------------
+template <typename T, int LD, int NP>
+__device__ bool warp_sweep_inverse(T *A, int n, T *rowk, T *inf_norm, int lane)
 {
-    const int nsh = delta > T(0) ? 2 : 1;
-    for (int s = 0; s < nsh; ++s) {
-        T sh = (nsh == 1) ? thr : (s == 0 ? thr + delta : thr - delta);
+    for (int k = 0; k < n; ++k) {
+        for (int j = lane; j < NP; j += 32) rowk[j] = (j < n) ? A[k * LD + j] : T(0);
         __syncwarp();
+        const T p = rowk[k];
+        if (!(p > T(0))) return false;
+        const T rp = T(1) / p;
         for (int i = lane; i < n; i += 32) {
-            for (int j = 0; j <= i; ++j) W[i * LD + j] = A[i * LD + j];
-            W[i * LD + i] -= sh;
+            T *Ai = A + i * LD;
+            if (i == k) {
+                for (int j = 0; j < n; ++j) Ai[j] = rowk[j] * rp;
+                Ai[k] = -rp;
+            } else {
+                const T f = rowk[i] * rp;
+                if (sizeof(T) == 4) {
+                    int j = 0;
+                    for (; j + 4 <= n; j += 4) {
+                        float4 r4 = *reinterpret_cast<const float4 *>(rowk + j);
+                        Ai[j] -= f * T(r4.x);
+                        Ai[j + 1] -= f * T(r4.y);
+                        Ai[j + 2] -= f * T(r4.z);
+                        Ai[j + 3] -= f * T(r4.w);
+                    }
+                    for (; j < n; ++j) Ai[j] -= f * rowk[j];
+                } else {
+                    for (int j = 0; j < n; ++j) Ai[j] -= f * rowk[j];
+                }
+                Ai[k] = f;
+            }
         }
         __syncwarp();
-        bool ok = warp_chol_r<T, LD>(W, n, lane);
-        __syncwarp();
-        if (nsh == 1) return ok ? 1 : -1;
-        if (s == 0 && ok) return 1;
-        if (s == 1 && !ok) return -1;
     }
-    return 0;
-}
-
-// inverse of a real SPD matrix from its Cholesky factor L (lower, in L):
-// X = L^{-T} L^{-1}; lane j solves column j (forward then back substitution).
-// X must not alias L.  Full symmetric X is written.
-template <typename T, int LD>
-__device__ void warp_chol_inverse_r(const T *L, T *X, int n, int lane)
-{
-    for (int j = lane; j < n; j += 32) {
-        // forward: L y = e_j ; y_i = 0 for i < j.  y stored in X[i][j].
-        for (int i = 0; i < j; ++i) X[i * LD + j] = T(0);
-        for (int i = j; i < n; ++i) {
-            T s = (i == j) ? T(1) : T(0);
-            for (int k = j; k < i; ++k) s -= L[i * LD + k] * X[k * LD + j];
-            X[i * LD + j] = s / L[i * LD + i];
+    T mx = T(0);
+    for (int i = lane; i < n; i += 32) {
+        T s = T(0);
+        for (int j = 0; j < n; ++j) {
+            T v = -A[i * LD + j];
+            A[i * LD + j] = v;
+            s += abs(v);
         }
-        // back: L^T x = y
-        for (int i = n - 1; i >= 0; --i) {
-            T s = X[i * LD + j];
-            for (int k = i + 1; k < n; ++k) s -= L[k * LD + i] * X[k * LD + j];
-            X[i * LD + j] = s / L[i * LD + i];
-        }
+        mx = max(mx, s);
     }
+    *inf_norm = warp_max(mx);
     __syncwarp();
+    return true;
 }
 
 // ------------------------------------------------------------------------
 // Householder tridiagonalisation (restates the zhetd2/zlarfg reduction):
 // Q^H A Q = T, Q = H(0)..H(n-2), reflector v_k in A[k+1.., k] (v_k[0] = 1),
 // tau_k in tau, d / e real.  A is full Hermitian storage, row i on lane i%32.
+// vv / ww: NP complex smem vectors (broadcast copies of v and w).
 // ------------------------------------------------------------------------
-template <typename T, int LD>
-__device__ void warp_tridiag(C2<T> *A, int n, T *d, T *e, C2<T> *tau, C2<T> *wv, int lane)
+template <typename T, int LD, int NP>
+__device__ void warp_tridiag(C2<T> *A, int n, T *d, T *e, C2<T> *tau, C2<T> *vv, C2<T> *ww, int lane)
 {
     for (int k = 0; k < n - 1; ++k) {
         T s = T(0);
         for (int i = k + 2 + lane; i < n; i += 32) s += cabs2(A[i * LD + k]);
         s = warp_sum(s);
-        C2<T> alpha = A[(k + 1) * LD + k];
+        const C2<T> alpha = A[(k + 1) * LD + k];
         C2<T> t = cmk<T>(T(0), T(0));
+        C2<T> scal = cmk<T>(T(1), T(0));
         T beta;
         if (s == T(0) && alpha.y == T(0)) {
             beta = alpha.x;
@@ -257,46 +326,81 @@ __device__ void warp_tridiag(C2<T> *A, int n, T *d, T *e, C2<T> *tau, C2<T> *wv,
             T nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + s);
             beta = alpha.x >= T(0) ? -nrm : nrm;
             t = cmk<T>((beta - alpha.x) / beta, -alpha.y / beta);
-            C2<T> scal = cdiv(cmk<T>(T(1), T(0)), cmk<T>(alpha.x - beta, alpha.y));
-            for (int i = k + 2 + lane; i < n; i += 32) A[i * LD + k] = cmul(A[i * LD + k], scal);
+            scal = cdiv(cmk<T>(T(1), T(0)), cmk<T>(alpha.x - beta, alpha.y));
         }
+        const bool act = (t.x != T(0) || t.y != T(0));
         __syncwarp();
+        // v: zeros up to k, 1 at k+1, scaled column below; kept in column k of A
+        for (int i = lane; i < NP; i += 32) {
+            C2<T> v = cmk<T>(T(0), T(0));
+            if (i == k + 1) v = cmk<T>(T(1), T(0));
+            else if (i > k + 1 && i < n) v = act ? cmul(A[i * LD + k], scal) : A[i * LD + k];
+            if (i > k && i < n) A[i * LD + k] = v;
+            vv[i] = v;
+        }
         if (lane == 0) {
-            A[(k + 1) * LD + k] = cmk<T>(T(1), T(0));
             tau[k] = t;
             e[k] = beta;
             d[k] = A[k * LD + k].x;
         }
         __syncwarp();
-        if (t.x != T(0) || t.y != T(0)) {
+        if (act) {
             // p = t * A22 v ; K = -1/2 t (p^H v) ; w = p + K v
-            C2<T> p0 = cmk<T>(T(0), T(0)), p1 = cmk<T>(T(0), T(0));
+            const int j0 = (k + 1) & ~1;
             C2<T> pv = cmk<T>(T(0), T(0));
-            int i0 = k + 1 + lane, i1 = i0 + 32;
-            if (i0 < n) {
-                C2<T> acc = cmk<T>(T(0), T(0));
-                for (int j = k + 1; j < n; ++j) acc = cadd(acc, cmul(A[i0 * LD + j], A[j * LD + k]));
-                p0 = cmul(t, acc);
-                pv = cadd(pv, ccmul(p0, A[i0 * LD + k]));
-            }
-            if (i1 < n) {
-                C2<T> acc = cmk<T>(T(0), T(0));
-                for (int j = k + 1; j < n; ++j) acc = cadd(acc, cmul(A[i1 * LD + j], A[j * LD + k]));
-                p1 = cmul(t, acc);
-                pv = cadd(pv, ccmul(p1, A[i1 * LD + k]));
+            C2<T> p[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int i = lane + 32 * h;
+                p[h] = cmk<T>(T(0), T(0));
+                if (h * 32 >= NP) continue;
+                if (i > k && i < n) {
+                    const C2<T> *Ai = A + i * LD;
+                    C2<T> acc0 = cmk<T>(T(0), T(0)), acc1 = cmk<T>(T(0), T(0));
+                    for (int j = j0; j < n; j += 2) {
+                        C2<T> v0, v1;
+                        if (sizeof(T) == 4) {
+                            float4 q = *reinterpret_cast<const float4 *>(vv + j);
+                            v0 = cmk<T>(T(q.x), T(q.y));
+                            v1 = cmk<T>(T(q.z), T(q.w));
+                        } else {
+                            v0 = vv[j];
+                            v1 = vv[j + 1];
+                        }
+                        cfma(acc0, Ai[j], v0);
+                        if (j + 1 < n) cfma(acc1, Ai[j + 1], v1);
+                    }
+                    p[h] = cmul(t, cadd(acc0, acc1));
+                    pv = cadd(pv, ccmul(p[h], vv[i]));
+                }
             }
             pv.x = warp_sum(pv.x);
             pv.y = warp_sum(pv.y);
-            C2<T> K = cscale(cmul(t, pv), T(-0.5));
-            if (i0 < n) wv[i0] = cadd(p0, cmul(K, A[i0 * LD + k]));
-            if (i1 < n) wv[i1] = cadd(p1, cmul(K, A[i1 * LD + k]));
+            const C2<T> K = cscale(cmul(t, pv), T(-0.5));
+            for (int i = lane; i < NP; i += 32) {
+                C2<T> w = cmk<T>(T(0), T(0));
+                if (i > k && i < n) w = cadd(p[i >= 32 ? 1 : 0], cmul(K, vv[i]));
+                ww[i] = w;
+            }
             __syncwarp();
-            // A22 -= v w^H + w v^H
+            // A22 -= v w^H + w v^H (vv / ww are zero at indices <= k)
             for (int i = k + 1 + lane; i < n; i += 32) {
-                C2<T> vi = A[i * LD + k], wi = wv[i];
-                for (int j = k + 1; j < n; ++j) {
-                    C2<T> vj = A[j * LD + k], wj = wv[j];
-                    A[i * LD + j] = csub(A[i * LD + j], cadd(cmulc(vi, wj), cmulc(wi, vj)));
+                C2<T> *Ai = A + i * LD;
+                const C2<T> vi = vv[i], wi = ww[i];
+                for (int j = j0; j < n; j += 2) {
+                    C2<T> v0, v1, w0, w1;
+                    if (sizeof(T) == 4) {
+                        float4 q = *reinterpret_cast<const float4 *>(vv + j);
+                        float4 r = *reinterpret_cast<const float4 *>(ww + j);
+                        v0 = cmk<T>(T(q.x), T(q.y));
+                        v1 = cmk<T>(T(q.z), T(q.w));
+                        w0 = cmk<T>(T(r.x), T(r.y));
+                        w1 = cmk<T>(T(r.z), T(r.w));
+                    } else {
+                        v0 = vv[j]; v1 = vv[j + 1]; w0 = ww[j]; w1 = ww[j + 1];
+                    }
+                    if (j > k) Ai[j] = csub(Ai[j], cadd(cmulc(vi, w0), cmulc(wi, v0)));
+                    if (j + 1 < n) Ai[j + 1] = csub(Ai[j + 1], cadd(cmulc(vi, w1), cmulc(wi, v1)));
                 }
             }
             __syncwarp();
@@ -315,7 +419,7 @@ __device__ __forceinline__ int sturm(const T *d, const T *e2, int n, T sigma, T 
     if (abs(q) <= pivmin) q = -pivmin;
     cnt += q < T(0);
     for (int i = 1; i < n; ++i) {
-        q = (d[i] - sigma) - e2[i - 1] / q;
+        q = (d[i] - sigma) - fdiv_fast(e2[i - 1], q);
         if (abs(q) <= pivmin) q = -pivmin;
         cnt += q < T(0);
     }
@@ -323,9 +427,11 @@ __device__ __forceinline__ int sturm(const T *d, const T *e2, int n, T sigma, T 
 }
 
 // index-th (1-based ascending) eigenvalue of the tridiagonal (d, e) by
-// 33-way warp multisection of the Gershgorin interval.
+// 33-way warp multisection.  [lo_hint, hi_hint] narrows the Gershgorin
+// interval when the caller knows a bound.
 template <typename T>
-__device__ T warp_tridiag_eig(const T *d, const T *e, T *e2, int n, int index, T *tnorm_out, int lane)
+__device__ T warp_tridiag_eig(const T *d, const T *e, T *e2, int n, int index, T lo_hint, T hi_hint,
+                              T *tnorm_out, int lane)
 {
     T gl = T(1e30), gu = T(-1e30), em = T(0);
     for (int i = lane; i < n; i += 32) {
@@ -340,24 +446,25 @@ __device__ T warp_tridiag_eig(const T *d, const T *e, T *e2, int n, int index, T
     em = warp_max(em);
     __syncwarp();
     const T eps = Eps<T>::v;
-    T pivmin = Eps<T>::tiny * max(T(1), em) * T(4);
-    T tnorm = max(abs(gl), abs(gu));
-    T fudge = T(2.1) * eps * tnorm * T(n) + T(2) * pivmin;
-    T lo = gl - fudge, hi = gu + fudge;
+    const T pivmin = Eps<T>::tiny * max(T(1), em) * T(4);
+    const T tnorm = max(abs(gl), abs(gu));
+    const T fudge = T(2.1) * eps * tnorm * T(n) + T(2) * pivmin;
+    T lo = max(gl - fudge, lo_hint), hi = min(gu + fudge, hi_hint);
+    if (!(lo < hi)) { lo = gl - fudge; hi = gu + fudge; }
     for (int it = 0; it < 64; ++it) {
-        T tol = T(2) * eps * max(abs(lo), abs(hi)) + pivmin;
+        const T tol = T(2) * eps * max(abs(lo), abs(hi)) + pivmin;
         if (hi - lo <= tol) break;
-        T w = (hi - lo) / T(33);
+        const T w = (hi - lo) / T(33);
         T sig = lo + w * T(lane + 1);
         if (lane == 31) sig = min(sig, hi);
-        int c = sturm(d, e2, n, sig, pivmin);
-        unsigned ge = __ballot_sync(0xffffffffu, c >= index);
-        int f = ge ? (__ffs(ge) - 1) : 32;        // first point with count >= index
-        T s_f = __shfl_sync(0xffffffffu, sig, f & 31);
-        T s_p = __shfl_sync(0xffffffffu, sig, (f - 1) & 31);
-        T nlo = (f == 0) ? lo : s_p;
-        T nhi = (f == 32) ? hi : s_f;
-        if (!(nhi < hi || nlo > lo)) break;       // no progress (rounding floor)
+        const int c = sturm(d, e2, n, sig, pivmin);
+        const unsigned ge = __ballot_sync(0xffffffffu, c >= index);
+        const int f = ge ? (__ffs(ge) - 1) : 32;        // first point with count >= index
+        const T s_f = __shfl_sync(0xffffffffu, sig, f & 31);
+        const T s_p = __shfl_sync(0xffffffffu, sig, (f - 1) & 31);
+        const T nlo = (f == 0) ? lo : s_p;
+        const T nhi = (f == 32) ? hi : s_f;
+        if (!(nhi < hi || nlo > lo)) break;            // no progress (rounding floor)
         lo = nlo;
         hi = nhi;
     }
@@ -373,54 +480,57 @@ __device__ void tridiag_inverse_iteration(const T *d, const T *e, int n, T lam, 
                                           T *wk, int lane)
 {
     if (lane == 0) {
-        T *dg = wk, *u1 = wk + n, *u2 = wk + 2 * n, *l = wk + 3 * n, *pv = wk + 4 * n;
+        T *rdg = wk, *u1 = wk + n, *u2 = wk + 2 * n, *l = wk + 3 * n, *pv = wk + 4 * n;
         const T eps = Eps<T>::v * (tnorm > T(0) ? tnorm : T(1));
-        for (int i = 0; i < n; ++i) {
-            dg[i] = d[i] - lam;
-            u1[i] = (i < n - 1) ? e[i] : T(0);
-            u2[i] = T(0);
-            l[i] = T(0);
-            pv[i] = T(0);
-        }
+        T dgi = d[0] - lam;
+        T u1i = (n > 1) ? e[0] : T(0);
+        T dnext = (n > 1) ? d[1] - lam : T(0);
+        T u1next = (n > 2) ? e[1] : T(0);
         for (int i = 0; i < n - 1; ++i) {
-            T sub = e[i];
-            if (abs(dg[i]) >= abs(sub)) {
-                if (dg[i] == T(0)) dg[i] = eps;
-                l[i] = sub / dg[i];
-                dg[i + 1] -= l[i] * u1[i];
+            const T sub = e[i];
+            T rd, ul1, ul2 = T(0), li, piv = T(0);
+            if (abs(dgi) >= abs(sub)) {
+                if (dgi == T(0)) dgi = eps;
+                rd = T(1) / dgi;
+                li = sub * rd;
+                ul1 = u1i;
+                dnext -= li * u1i;          // next row keeps u1next
             } else {
-                T mult = dg[i] / sub;
-                T old_u1 = u1[i];
-                dg[i] = sub;
-                u1[i] = dg[i + 1];
-                u2[i] = (i < n - 2) ? u1[i + 1] : T(0);
-                dg[i + 1] = old_u1 - mult * u1[i];
-                if (i < n - 2) u1[i + 1] = -mult * u2[i];
-                l[i] = mult;
-                pv[i] = T(1);
+                const T mult = dgi / sub;
+                rd = T(1) / sub;
+                ul1 = dnext;
+                ul2 = u1next;
+                const T nd = u1i - mult * dnext;
+                u1next = -mult * u1next;
+                dnext = nd;
+                li = mult;
+                piv = T(1);
             }
+            rdg[i] = rd; u1[i] = ul1; u2[i] = ul2; l[i] = li; pv[i] = piv;
+            dgi = dnext;
+            u1i = u1next;
+            dnext = (i + 2 < n) ? d[i + 2] - lam : T(0);
+            u1next = (i + 3 < n) ? e[i + 2] : T(0);
         }
-        if (dg[n - 1] == T(0)) dg[n - 1] = eps;
-        unsigned s = 12345u;
-        for (int i = 0; i < n; ++i) {
-            s = s * 1103515245u + 12345u;
-            y[i] = T((s >> 8) & 0xFFFF) / T(65535) + T(0.5);
-        }
-        for (int it = 0; it < 3; ++it) {
+        if (dgi == T(0)) dgi = eps;
+        rdg[n - 1] = T(1) / dgi;
+        u1[n - 1] = T(0); u2[n - 1] = T(0);
+        for (int i = 0; i < n; ++i) y[i] = T(1);
+        for (int it = 0; it < 2; ++it) {
             for (int i = 0; i < n - 1; ++i) {
                 if (pv[i] != T(0)) { T t = y[i]; y[i] = y[i + 1]; y[i + 1] = t - l[i] * y[i]; }
                 else y[i + 1] -= l[i] * y[i];
             }
+            T y1 = T(0), y2 = T(0), mx = T(0);
             for (int i = n - 1; i >= 0; --i) {
-                T t = y[i];
-                if (i + 1 < n) t -= u1[i] * y[i + 1];
-                if (i + 2 < n) t -= u2[i] * y[i + 2];
-                y[i] = t / dg[i];
+                T t = (y[i] - u1[i] * y1 - u2[i] * y2) * rdg[i];
+                y[i] = t;
+                y2 = y1;
+                y1 = t;
+                mx = max(mx, abs(t));
             }
-            T mx = T(0);
-            for (int i = 0; i < n; ++i) mx = max(mx, abs(y[i]));
             if (!(mx > T(0)) || !isfinite(mx)) { for (int i = 0; i < n; ++i) y[i] = T(1); continue; }
-            T r = T(1) / mx;
+            const T r = T(1) / mx;
             for (int i = 0; i < n; ++i) y[i] *= r;
         }
     }
@@ -430,8 +540,8 @@ __device__ void tridiag_inverse_iteration(const T *d, const T *e, int n, T lam, 
 // Eigenpair of the Hermitian matrix in W (destroyed): index-th eigenvalue
 // (1-based ascending).  Returns the eigenvalue; lane i gets z_i (and z_{i+32}).
 template <typename T, int NP>
-__device__ T warp_eigpair(C2<T> *W, int n, int index, unsigned char *sm, int lane,
-                          C2<T> &z0, C2<T> &z1)
+__device__ T warp_eigpair(C2<T> *W, int n, int index, T lo_hint, T hi_hint, unsigned char *sm,
+                          int lane, C2<T> &z0, C2<T> &z1)
 {
     using L = Lay<T, NP>;
     constexpr int LD = L::LD;
@@ -439,34 +549,207 @@ __device__ T warp_eigpair(C2<T> *W, int n, int index, unsigned char *sm, int lan
     T *e = reinterpret_cast<T *>(sm + L::ee);
     T *e2 = reinterpret_cast<T *>(sm + L::e2);
     T *y = reinterpret_cast<T *>(sm + L::yy);
-    T *wk = reinterpret_cast<T *>(sm + L::lr);   // free while the eigenpair is computed
+    T *wk = reinterpret_cast<T *>(sm + L::wk);
     C2<T> *tau = reinterpret_cast<C2<T> *>(sm + L::tu);
-    C2<T> *wv = reinterpret_cast<C2<T> *>(sm + L::vw);
+    C2<T> *vv = reinterpret_cast<C2<T> *>(sm + L::vv);
+    C2<T> *ww = reinterpret_cast<C2<T> *>(sm + L::ww);
     if (n == 1) {
         z0 = cmk<T>(T(1), T(0));
         z1 = cmk<T>(T(0), T(0));
         return W[0].x;
     }
-    warp_tridiag<T, LD>(W, n, d, e, tau, wv, lane);
+    warp_tridiag<T, LD, NP>(W, n, d, e, tau, vv, ww, lane);
     T tnorm;
-    T lam = warp_tridiag_eig<T>(d, e, e2, n, index, &tnorm, lane);
+    const T lam = warp_tridiag_eig<T>(d, e, e2, n, index, lo_hint, hi_hint, &tnorm, lane);
     tridiag_inverse_iteration<T>(d, e, n, lam, tnorm, y, wk, lane);
-    int i0 = lane, i1 = lane + 32;
+    const int i0 = lane, i1 = lane + 32;
     z0 = (i0 < n) ? cmk<T>(y[i0], T(0)) : cmk<T>(T(0), T(0));
     z1 = (i1 < n) ? cmk<T>(y[i1], T(0)) : cmk<T>(T(0), T(0));
     for (int k = n - 2; k >= 0; --k) {
-        C2<T> t = tau[k];
+        const C2<T> t = tau[k];
         if (t.x == T(0) && t.y == T(0)) continue;
         C2<T> s = cmk<T>(T(0), T(0));
         if (i0 >= k + 1 && i0 < n) s = cadd(s, ccmul(W[i0 * LD + k], z0));
-        if (i1 >= k + 1 && i1 < n) s = cadd(s, ccmul(W[i1 * LD + k], z1));
+        if (NP > 32 && i1 >= k + 1 && i1 < n) s = cadd(s, ccmul(W[i1 * LD + k], z1));
         s.x = warp_sum(s.x);
         s.y = warp_sum(s.y);
         s = cmul(t, s);
         if (i0 >= k + 1 && i0 < n) z0 = csub(z0, cmul(s, W[i0 * LD + k]));
-        if (i1 >= k + 1 && i1 < n) z1 = csub(z1, cmul(s, W[i1 * LD + k]));
+        if (NP > 32 && i1 >= k + 1 && i1 < n) z1 = csub(z1, cmul(s, W[i1 * LD + k]));
     }
     return lam;
+}
+
+// Largest eigenvector of the Hermitian C by power iteration.  Returns true
+// with z (lane-distributed) when the residual test passes; false when the
+// iteration converges too slowly (the caller then uses the Householder path).
+template <typename T, int NP>
+__device__ bool warp_power(const C2<T> *C, int n, unsigned char *sm, int lane, C2<T> &z0, C2<T> &z1,
+                           T *lam_out)
+{
+    using L = Lay<T, NP>;
+    constexpr int LD = L::LD;
+    C2<T> *vv = reinterpret_cast<C2<T> *>(sm + L::vv);
+    const int i0 = lane, i1 = lane + 32;
+    // start: row sums (C * 1)
+    for (int i = lane; i < NP; i += 32) vv[i] = cmk<T>(i < n ? T(1) : T(0), T(0));
+    __syncwarp();
+    T rprev = T(-1);
+    const T tol = (sizeof(T) == 4) ? T(4e-6) : T(1e-13);
+    for (int it = 0; it < 96; ++it) {
+        C2<T> u[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = lane + 32 * h;
+            u[h] = cmk<T>(T(0), T(0));
+            if (h * 32 >= NP || i >= n) continue;
+            const C2<T> *Ci = C + i * LD;
+            C2<T> a0 = cmk<T>(T(0), T(0)), a1 = cmk<T>(T(0), T(0));
+            for (int j = 0; j < n; j += 2) {
+                C2<T> v0, v1;
+                if (sizeof(T) == 4) {
+                    float4 q = *reinterpret_cast<const float4 *>(vv + j);
+                    v0 = cmk<T>(T(q.x), T(q.y));
+                    v1 = cmk<T>(T(q.z), T(q.w));
+                } else {
+                    v0 = vv[j];
+                    v1 = vv[j + 1];
+                }
+                cfma(a0, Ci[j], v0);
+                if (j + 1 < n) cfma(a1, Ci[j + 1], v1);
+            }
+            u[h] = cadd(a0, a1);
+        }
+        // rho = v^H u (v normalised after the first pass), residual u - rho v
+        const C2<T> v0 = (i0 < n) ? vv[i0] : cmk<T>(T(0), T(0));
+        const C2<T> v1 = (NP > 32 && i1 < n) ? vv[i1] : cmk<T>(T(0), T(0));
+        T vn = warp_sum(cabs2(v0) + cabs2(v1));
+        T rho = warp_sum(ccmul(v0, u[0]).x + ccmul(v1, u[1]).x) / vn;
+        const C2<T> r0 = csub(u[0], cscale(v0, rho)), r1 = csub(u[1], cscale(v1, rho));
+        const T rn = sqrt(warp_sum(cabs2(r0) + cabs2(r1)) / vn);
+        const T un = warp_sum(cabs2(u[0]) + cabs2(u[1]));
+        const T inv = rsqrt_t(un);
+        __syncwarp();
+        if (i0 < n) vv[i0] = cscale(u[0], inv);
+        if (NP > 32 && i1 < n) vv[i1] = cscale(u[1], inv);
+        __syncwarp();
+        // eigenvector error ~ rn / gap; the contraction rn/rprev estimates
+        // lambda2/lambda1, so the gap is about rho (1 - ratio)
+        const T ratio = (rprev > T(0)) ? min(rn / rprev, T(1)) : T(1);
+        rprev = rn;
+        if (it >= 2 && rn <= tol * rho * max(T(1) - ratio, T(0.05))) {
+            z0 = (i0 < n) ? vv[i0] : cmk<T>(T(0), T(0));
+            z1 = (NP > 32 && i1 < n) ? vv[i1] : cmk<T>(T(0), T(0));
+            *lam_out = rho;
+            return true;
+        }
+        if (it >= 8 && ratio > T(0.8)) return false;   // slow: use the Householder path
+    }
+    return false;
+}
+
+// y = A x for the Hermitian A in smem (lane-distributed x / y)
+template <typename T, int LD, int NP>
+__device__ void warp_matvec(const C2<T> *A, int n, const C2<T> *xv, C2<T> &y0, C2<T> &y1, int lane)
+{
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int i = lane + 32 * h;
+        C2<T> u = cmk<T>(T(0), T(0));
+        if (h * 32 < NP && i < n) {
+            const C2<T> *Ai = A + i * LD;
+            C2<T> a0 = cmk<T>(T(0), T(0)), a1 = cmk<T>(T(0), T(0));
+#pragma unroll 2
+            for (int j = 0; j < n; j += 2) {
+                C2<T> v0, v1;
+                if (sizeof(T) == 4) {
+                    const float4 q = *reinterpret_cast<const float4 *>(xv + j);
+                    v0 = cmk<T>(T(q.x), T(q.y));
+                    v1 = cmk<T>(T(q.z), T(q.w));
+                } else {
+                    v0 = xv[j];
+                    v1 = xv[j + 1];
+                }
+                cfma(a0, Ai[j], v0);
+                if (j + 1 < n) cfma(a1, Ai[j + 1], v1);
+            }
+            u = cadd(a0, a1);
+        }
+        if (h == 0) y0 = u; else y1 = u;
+    }
+}
+
+// A few power iterations on C from the all-ones vector: a start vector for
+// the MLE inverse iteration (the EVD and MLE solutions are close).  Leaves
+// the normalised vector lane-distributed in z0 / z1 and in vv.
+template <typename T, int NP>
+__device__ void warp_power_start(const C2<T> *C, int n, int iters, unsigned char *sm, int lane,
+                                 C2<T> &z0, C2<T> &z1)
+{
+    using L = Lay<T, NP>;
+    C2<T> *vv = reinterpret_cast<C2<T> *>(sm + L::vv);
+    for (int i = lane; i < NP; i += 32) vv[i] = cmk<T>(i < n ? T(1) : T(0), T(0));
+    __syncwarp();
+    for (int it = 0; it < iters; ++it) {
+        C2<T> u0, u1;
+        warp_matvec<T, L::LD, NP>(C, n, vv, u0, u1, lane);
+        const T inv = rsqrt_t(warp_sum(cabs2(u0) + cabs2(u1)));
+        z0 = cscale(u0, inv);
+        z1 = cscale(u1, inv);
+        __syncwarp();
+        if (lane < n) vv[lane] = z0;
+        if (NP > 32 && lane + 32 < n) vv[lane + 32] = z1;
+        __syncwarp();
+    }
+}
+
+// Smallest eigenpair of the Hermitian M (in W, destroyed) by inverse
+// iteration with the shift sigma.  A successful Cholesky factorisation of
+// M - sigma I certifies sigma < lambda_1, so the iteration converges to the
+// smallest eigenpair; its rate is (lambda_1 - sigma) / (lambda_2 - sigma).
+// The start vector comes in z0 / z1.  Returns 1 when converged (z = unit
+// eigenvector, *lam = Rayleigh quotient), 0 when converging too slowly, -1
+// when M - sigma I is not positive definite.
+template <typename T, int NP>
+__device__ int warp_inverse_iteration(C2<T> *W, int n, T sigma, unsigned char *sm, int lane,
+                                      C2<T> &z0, C2<T> &z1, T *lam)
+{
+    using L = Lay<T, NP>;
+    constexpr int LD = L::LD;
+    C2<T> *col = reinterpret_cast<C2<T> *>(sm + L::ww);
+    for (int i = lane; i < n; i += 32) W[i * LD + i].x -= sigma;
+    __syncwarp();
+    if (!warp_chol_c<T, LD, NP, true>(W, n, col, lane)) return -1;
+    T rprev = T(-1), cmin = T(1);
+    for (int it = 0; it < 12; ++it) {
+        C2<T> x0 = z0, x1 = z1;
+        warp_chol_solve<T, LD, NP>(W, n, x0, x1, lane);
+        const T xx = warp_sum(cabs2(x0) + cabs2(x1));
+        const T xv = warp_sum(ccmul(x0, z0).x + ccmul(x1, z1).x);
+        const T rho = sigma + xv / xx;
+        // M x - rho x = z + (sigma - rho) x
+        const C2<T> r0 = cadd(z0, cscale(x0, sigma - rho)), r1 = cadd(z1, cscale(x1, sigma - rho));
+        const T inv = rsqrt_t(xx);
+        const T rn = sqrt(warp_sum(cabs2(r0) + cabs2(r1))) * inv;
+        z0 = cscale(x0, inv);
+        z1 = cscale(x1, inv);
+        T c = T(1);
+        if (rprev > T(0)) {
+            c = rn / rprev;
+            cmin = min(cmin, c);
+        }
+        rprev = rn;
+        *lam = rho;
+        if (it >= 1 && cmin < T(1)) {
+            // eigenvector error ~ rn / (lambda_2 - lambda_1); the contraction
+            // estimates the gap: lambda_2 - lambda_1 ~ (rho - sigma)(1/c - 1)
+            const T gap = (rho - sigma) * (T(1) / cmin - T(1));
+            const T tol = (sizeof(T) == 4) ? T(1e-5) : T(1e-12);
+            if (rn <= tol * gap) return 1;
+            if (it >= 2 && c > T(0.5) && rn <= T(20) * tol * gap) return 1;   // rounding floor
+        }
+    }
+    return 0;
 }
 
 // ------------------------------------------------------------------------
@@ -496,13 +779,20 @@ __device__ __forceinline__ void acc_prod<double>(C2<double> &acc, float2 a, floa
     acc.y += double(im);
 }
 
-template <typename T>
 __device__ __forceinline__ void defer_fp64(const KParams &P, long long pp, int lane)
 {
     if (lane == 0) {
         int idx = atomicAdd(P.fb_count, 1);
         if (idx < P.fb_cap) P.fb_list[idx] = pp;
         else atomicOr(P.err, ERR_FB_OVERFLOW);
+    }
+}
+
+__device__ __forceinline__ void put_code(const KParams &P, long long pp, int lane, int code)
+{
+    if (lane == 0) {
+        P.tcorr[pp] = float(code);
+        if (P.status) P.status[pp] = code;
     }
 }
 
@@ -521,9 +811,9 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
     C2<T> *Cm = reinterpret_cast<C2<T> *>(sm + L::cm);
     C2<T> *Wm = reinterpret_cast<C2<T> *>(sm + L::wm);
     float2 *Xs = reinterpret_cast<float2 *>(sm + L::wm);
-    T *Lr = reinterpret_cast<T *>(sm + L::lr);
     T *Xr = reinterpret_cast<T *>(sm + L::xr);
     T *yv = reinterpret_cast<T *>(sm + L::yy);
+    C2<T> *col = reinterpret_cast<C2<T> *>(sm + L::vv);
     float2 *phs = reinterpret_cast<float2 *>(sm + L::ph);
 
     const int n = P.nb;
@@ -593,7 +883,10 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
             const float2 *src = P.stack + q;
             float2 *dst = Xs + rk * XS;
 #pragma unroll 4
-            for (int t = 0; t < n; ++t) dst[t] = __ldg(src + t * plane);
+            for (int t = 0; t < n; ++t) {
+                dst[t] = __ldg(src);
+                src += plane;
+            }
         }
         __syncwarp();
         npix += cnt;
@@ -690,16 +983,13 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
         if (bad) {
             // non-finite coherence: LAPACK's answer on NaN input is undefined;
             // the first eigen call is reported as failed.
-            int code = (!plink && P.method != M_MLE) ? -6 : -1;
-            if (lane == 0) {
-                P.tcorr[pp] = float(code);
-                if (P.status) P.status[pp] = code;
-            }
+            put_code(P, pp, lane, (!plink && P.method != M_MLE) ? -6 : -1);
             return;
         }
     }
 
-    const T amb = T(P.amb) * T(n) * Eps<T>::v;          // 0 in the FP64 form
+    const bool fp32 = sizeof(T) == 4;
+    const T amb = T(P.amb) * T(n) * Eps<T>::v;          // rounding band unit (FP32 only)
     const T thr = T(1.0e-6);
     int mode = 0;       // 0 = MLE eigvec of M, 1 = largest eigvec of C
     int pstatus = 0;
@@ -710,13 +1000,29 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
             for (int j = 0; j < nn; ++j) s += cabs2(A[i * LD + j]);
         return sqrt(warp_sum(s));
     };
-    auto fill_absC = [&]() {
-        for (int i = lane; i < nn; i += 32)
-            for (int j = 0; j < nn; ++j)
-                Lr[i * LD + j] = (i == j) ? T(1) : sqrt(cabs2(Cm[i * LD + j]));
+    // |C| into Xr (unit diagonal), then its sweep inverse.  Returns
+    // +1 inverted (X = inv|C| in Xr), -1 not positive definite, 0 undecided
+    // in FP32 (rounding band or condition too large).
+    auto abs_inverse = [&]() -> int {
+        T rs = T(0);
+        for (int i = lane; i < nn; i += 32) {
+            T s = T(0);
+            for (int j = 0; j < nn; ++j) {
+                T a = (i == j) ? T(1) : sqrt(cabs2(Cm[i * LD + j]));
+                Xr[i * LD + j] = a;
+                s += a;
+            }
+            rs = max(rs, s);
+        }
+        const T anorm = warp_max(rs);          // |C| inf-norm
         __syncwarp();
+        T xnorm;
+        bool ok = warp_sweep_inverse<T, LD, NP>(Xr, nn, yv, &xnorm, lane);
+        if (!fp32) return ok ? 1 : -1;
+        if (!ok) return 0;                     // FP32 pivot failure: settle in FP64
+        if (!(anorm * xnorm <= T(P.cond_max))) return 0;
+        return 1;
     };
-    const bool fp32 = sizeof(T) == 4;
 
     if (!plink) {
         if (P.method == M_MLE) {
@@ -725,31 +1031,60 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
                 // fewer SHPs than dates: Gamma has rank <= npix < n, so its
                 // smallest eigenvalue is 0 up to FP32 product rounding (far
                 // below 1e-6): the reference reports -2.
-                if (lane == 0) { P.tcorr[pp] = -2.f; if (P.status) P.status[pp] = -2; }
+                put_code(P, pp, lane, -2);
                 return;
             }
-            T dC = fp32 ? amb * fro(Cm) : T(0);
-            int r = lam_min_test_c<T, LD>(Cm, Wm, n, thr, dC, lane);
-            if (r == 0) { defer_fp64<T>(P, pp, lane); return; }
-            if (r < 0) { if (lane == 0) { P.tcorr[pp] = -2.f; if (P.status) P.status[pp] = -2; } return; }
-            fill_absC();
-            T sA = T(0);
-            if (fp32) {
-                T s = T(0);
-                for (int i = lane; i < n; i += 32)
-                    for (int j = 0; j < n; ++j) s += Lr[i * LD + j] * Lr[i * LD + j];
-                sA = amb * sqrt(warp_sum(s));
-            }
-            r = lam_min_test_r<T, LD>(Lr, Xr, n, thr, sA, lane);
-            if (r == 0) { defer_fp64<T>(P, pp, lane); return; }
-            if (r < 0) { if (lane == 0) { P.tcorr[pp] = -4.f; if (P.status) P.status[pp] = -4; } return; }
-            // |C| is positive definite with margin: factor and invert (evd.cpp:652-664)
-            if (!warp_chol_r<T, LD>(Lr, n, lane)) {
-                if (fp32) { defer_fp64<T>(P, pp, lane); return; }
-                if (lane == 0) { P.tcorr[pp] = -5.f; if (P.status) P.status[pp] = -5; }
+            const T dC = fp32 ? amb * fro(Cm) : T(0);
+            int r = lam_min_test_c<T, LD, NP>(Cm, Wm, col, n, thr, dC, lane);
+            if (r == 0) { defer_fp64(P, pp, lane); return; }
+            if (r < 0) { put_code(P, pp, lane, -2); return; }
+            // |C| check (evd.cpp:623-644) and inverse (evd.cpp:652-664).
+            // lambda_min(|C|) >= 1 / ||inv|C|||_inf, so a small inverse norm
+            // settles the 1e-6 test; anything else is settled in FP64.
+            r = abs_inverse();
+            if (r == 0) { defer_fp64(P, pp, lane); return; }
+            if (r < 0) {
+                // FP64: not positive definite, so lambda_min(|C|) <= 0 < 1e-6
+                put_code(P, pp, lane, -4);
                 return;
             }
-            warp_chol_inverse_r<T, LD>(Lr, Xr, n, lane);
+            if (!fp32) {
+                // lambda_min(|C|) >= 1/||inv|C|||_inf settles the 1e-6 test
+                // unless the inverse is large
+                T xn = T(0);
+                for (int i = lane; i < n; i += 32) {
+                    T s = T(0);
+                    for (int j = 0; j < n; ++j) s += abs(Xr[i * LD + j]);
+                    xn = max(xn, s);
+                }
+                xn = warp_max(xn);
+                if (!(xn < T(1) / thr)) {
+                    // decide with the Cholesky test of |C| - 1e-6 I (this work
+                    // matrix overlaps the inverse, which is then recomputed)
+                    __syncwarp();
+                    for (int i = lane; i < n; i += 32) {
+                        for (int j = 0; j <= i; ++j)
+                            Wm[i * LD + j] = cmk<T>((i == j) ? T(1) - thr : sqrt(cabs2(Cm[i * LD + j])), T(0));
+                    }
+                    __syncwarp();
+                    if (!warp_chol_c<T, LD, NP>(Wm, n, col, lane)) {
+                        put_code(P, pp, lane, -4);
+                        return;
+                    }
+                    __syncwarp();
+                    abs_inverse();
+                }
+            } else {
+                T xn = T(0);
+                for (int i = lane; i < n; i += 32) {
+                    T s = T(0);
+                    for (int j = 0; j < n; ++j) s += abs(Xr[i * LD + j]);
+                    xn = max(xn, s);
+                }
+                xn = warp_max(xn);
+                const T dA = amb * T(n);
+                if (!(T(1) / xn > thr + dA)) { defer_fp64(P, pp, lane); return; }
+            }
             mode = 0;
         } else {
             if (P.method == M_STBAS) {                       // evd.cpp:695-706
@@ -762,18 +1097,9 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
         }
     } else {
         // phase_link.cpp:540-618: MLE if |C| is invertible, else EVD
-        fill_absC();
-        T sA = T(0);
-        if (fp32) {
-            T s = T(0);
-            for (int i = lane; i < n; i += 32)
-                for (int j = 0; j < n; ++j) s += Lr[i * LD + j] * Lr[i * LD + j];
-            sA = amb * sqrt(warp_sum(s));
-        }
-        int r = lam_min_test_r<T, LD>(Lr, Xr, n, T(0), sA, lane);
-        if (r == 0) { defer_fp64<T>(P, pp, lane); return; }
-        if (r > 0 && warp_chol_r<T, LD>(Lr, n, lane)) {
-            warp_chol_inverse_r<T, LD>(Lr, Xr, n, lane);
+        int r = abs_inverse();
+        if (r == 0) { defer_fp64(P, pp, lane); return; }
+        if (r > 0) {
             mode = 0;
         } else {
             mode = 1;
@@ -784,27 +1110,76 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
     // ---- the eigenvector --------------------------------------------------
     C2<T> z0, z1;
     if (mode == 0) {
-        // M = inv(|C|) o C (evd.cpp:667) ; smallest eigenpair (evd.cpp:670-686)
-        for (int i = lane; i < n; i += 32)
-            for (int j = 0; j < n; ++j) Wm[i * LD + j] = cscale(Cm[i * LD + j], Xr[i * LD + j]);
+        // M = inv(|C|) o C (evd.cpp:667); Xr shares bytes with Wm, so each
+        // lane reads its inverse row into registers before M is written.
+        auto form_M = [&]() {
+            for (int base = 0; base < nn; base += 32) {
+                const int i = base + lane;
+                T xrow[NP];
+#pragma unroll
+                for (int j = 0; j < NP; ++j) xrow[j] = (i < nn && j < nn) ? Xr[i * LD + j] : T(0);
+                __syncwarp();
+                if (i < nn) {
+#pragma unroll
+                    for (int j = 0; j < NP; ++j)
+                        if (j < nn) Wm[i * LD + j] = cscale(Cm[i * LD + j], xrow[j]);
+                }
+                __syncwarp();
+            }
+        };
+        form_M();
+        // smallest eigenpair (evd.cpp:670-686).  M = inv|C| o C is positive
+        // semi-definite (Schur product), and its smallest eigenvalue is at
+        // most the mean of its diagonal.
+        T tr = T(0);
+        for (int i = lane; i < n; i += 32) tr += Wm[i * LD + i].x;
+        tr = warp_sum(tr) / T(n);
+        const T dM = (fp32 && !plink) ? amb * fro(Wm) : T(0);
         __syncwarp();
-        T dM = T(0);
-        if (fp32 && !plink) dM = amb * fro(Wm);
-        __syncwarp();
-        T lam = warp_eigpair<T, NP>(Wm, n, 1, sm, lane, z0, z1);
-        if (!plink) {
-            if (lam < thr + dM && lam >= thr - dM && fp32) { defer_fp64<T>(P, pp, lane); return; }
-            if (lam < thr) { if (lane == 0) { P.tcorr[pp] = -7.f; if (P.status) P.status[pp] = -7; } return; }
+        bool done = false;
+        if (fp32) {
+            // inverse iteration from the EVD direction, shifted just below
+            // the Rayleigh quotient (the smallest eigenvalue is close to 1)
+            warp_power_start<T, NP>(Cm, n, 4, sm, lane, z0, z1);
+            C2<T> *vv = reinterpret_cast<C2<T> *>(sm + L::vv);
+            C2<T> m0, m1;
+            warp_matvec<T, LD, NP>(Wm, n, vv, m0, m1, lane);
+            const T rho0 = warp_sum(ccmul(z0, m0).x + ccmul(z1, m1).x);
+            const T sigma = T(0.98) * min(rho0, T(1));
+            __syncwarp();
+            if (sigma > thr + dM) {
+                T lam;
+                const int st = warp_inverse_iteration<T, NP>(Wm, n, sigma, sm, lane, z0, z1, &lam);
+                if (st == 1) {
+                    done = true;   // lambda_1 > sigma > 1e-6 + band: the -7 test passes
+                } else {
+                    if (lane == 0) atomicAdd(P.slow, 1);
+                    __syncwarp();
+                    abs_inverse();  // rebuild M for the Householder path
+                    form_M();
+                }
+            }
+        }
+        if (!done) {
+            const T lam = warp_eigpair<T, NP>(Wm, n, 1, T(-1e30), tr * T(1.0001), sm, lane, z0, z1);
+            if (!plink) {
+                if (fp32 && lam < thr + dM && lam >= thr - dM) { defer_fp64(P, pp, lane); return; }
+                if (lam < thr) { put_code(P, pp, lane, -7); return; }
+            }
         }
     } else {
-        for (int i = lane; i < n; i += 32)
-            for (int j = 0; j < n; ++j) Wm[i * LD + j] = Cm[i * LD + j];
-        __syncwarp();
-        T lam = warp_eigpair<T, NP>(Wm, n, n, sm, lane, z0, z1);
-        if (!plink && lam < thr) {                           // evd.cpp:718-726
-            if (lane == 0) { P.tcorr[pp] = -7.f; if (P.status) P.status[pp] = -7; }
-            return;
+        T lam;
+        bool ok = warp_power<T, NP>(Cm, n, sm, lane, z0, z1, &lam);
+        if (!ok) {
+            if (lane == 0 && fp32) atomicAdd(P.slow, 1);
+            for (int i = lane; i < n; i += 32)
+                for (int j = 0; j < n; ++j) Wm[i * LD + j] = Cm[i * LD + j];
+            __syncwarp();
+            lam = warp_eigpair<T, NP>(Wm, n, n, T(0.999), T(1e30), sm, lane, z0, z1);
         }
+        // trace(C) = n, so lambda_max >= 1: the -7 test of evd.cpp:718-726
+        // cannot trigger for a finite C.
+        if (!plink && lam < thr) { put_code(P, pp, lane, -7); return; }
     }
 
     // ---- phase referencing (evd.cpp:738-749) ------------------------------
@@ -815,16 +1190,16 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
         zr.x = __shfl_sync(0xffffffffu, a.x, mref & 31);
         zr.y = __shfl_sync(0xffffffffu, a.y, mref & 31);
     }
-    const T zra = sqrt(cabs2(zr));
-    const C2<T> zru = (zra > T(0)) ? cscale(zr, T(1) / zra) : cmk<T>(T(1), T(0));
+    const T zra2 = cabs2(zr);
+    const C2<T> zru = (zra2 > T(0)) ? cscale(zr, rsqrt_t(zra2)) : cmk<T>(T(1), T(0));
     float2 ph0 = make_float2(0.f, 0.f), ph1 = make_float2(0.f, 0.f);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int i = lane + 32 * h;
         if (i >= n) continue;
         C2<T> z = h ? z1 : z0;
-        T za = sqrt(cabs2(z));
-        C2<T> u = (za > T(0)) ? cscale(z, T(1) / za) : cmk<T>(T(1), T(0));
+        T za2 = cabs2(z);
+        C2<T> u = (za2 > T(0)) ? cscale(z, rsqrt_t(za2)) : cmk<T>(T(1), T(0));
         C2<T> pr = cmulc(u, zru);                       // exp(i(arg z_i - arg z_ref))
         float2 o = (i == mref) ? make_float2(1.f, 0.f) : make_float2(float(pr.x), float(pr.y));
         if (h) ph1 = o; else ph0 = o;
@@ -861,16 +1236,16 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
         T sr = T(0), si = T(0);
         int cnt = 0;
         for (int i = lane; i < n; i += 32) {
-            int ulim = stbas ? min(i + P.bw + 1, n) : n;
+            const int ulim = stbas ? min(i + P.bw + 1, n) : n;
             const float2 pi = phs[i];
             const C2<T> cpi = cmk<T>(T(pi.x), T(pi.y));
             for (int j = i + 1; j < ulim; ++j) {
-                C2<T> c = Cm[i * LD + j];
-                T ca = sqrt(cabs2(c));
-                C2<T> u = (ca > T(0)) ? cscale(c, T(1) / ca) : cmk<T>(T(1), T(0));
+                const C2<T> c = Cm[i * LD + j];
+                const T ca2 = cabs2(c);
+                const C2<T> u = (ca2 > T(0)) ? cscale(c, rsqrt_t(ca2)) : cmk<T>(T(1), T(0));
                 const float2 pj = phs[j];
                 // exp(i(arg C_ij - arg ph_i + arg ph_j))
-                C2<T> v = cmul(cmulc(u, cpi), cmk<T>(T(pj.x), T(pj.y)));
+                const C2<T> v = cmul(cmulc(u, cpi), cmk<T>(T(pj.x), T(pj.y)));
                 sr += v.x;
                 si += v.y;
                 cnt++;
