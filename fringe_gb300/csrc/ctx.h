@@ -8,6 +8,10 @@
 
 #include "fringe_gb300.h"
 
+// default tuning of the FP32 form
+constexpr float kDefaultAmbScale = 8.0f;    // FP32 rounding band, in units of n*eps*|A|_F
+constexpr float kDefaultCondMax = 1000.0f;  // |C| inverted in FP32 up to this inf-norm condition
+
 struct fpl_ctx {
     int device = 0;
     int num_sms = 0;
@@ -23,8 +27,8 @@ struct fpl_ctx {
     size_t cap_fb_list = 0;
     void *d_small = nullptr;
     // tuning
-    float amb_scale = 8.0f;
-    float cond_max = 1000.0f;   // |C| inverted in FP32 up to this inf-norm condition
+    float amb_scale = kDefaultAmbScale;
+    float cond_max = kDefaultCondMax;
     bool force_fp64 = false;
     // optional per-kernel timing: one event triple per enqueued run
     bool profile = false;
