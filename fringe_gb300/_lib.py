@@ -59,6 +59,7 @@ _SIGS = {
     "fpl_process": (ctypes.c_int, [ctypes.POINTER(FplOptions)]),
     "fpl_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "fpl_version": (ctypes.c_char_p, []),
+    "fpl_run_noalloc": (ctypes.c_int, [ctypes.POINTER(FplJob), _P]),
     "fpl_ctx_set_tuning": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
     "fpl_ctx_last_error": (ctypes.c_char_p, [_P]),
     "fpl_ctx_set_profiling": (ctypes.c_int, [_P, ctypes.c_int]),

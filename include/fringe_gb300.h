@@ -86,6 +86,7 @@ enum fpl_pixel_status {
 #define FPL_ERR_UNSUPPORTED    203   /* nbands > 64 or window > 1024 taps */
 #define FPL_ERR_DEVICE_CHECK   204   /* a kernel reported an internal error */
 #define FPL_ERR_NULL           205   /* a required pointer is NULL */
+#define FPL_ERR_NOALLOC_LIMIT  206   /* job larger than fpl_run_noalloc's scratch */
 
 #define FPL_MAX_BANDS 64
 #define FPL_MAX_NULONG 32
@@ -146,6 +147,21 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job);
 int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream);
 
 int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out);
+
+/* ---- run without device allocation (no counterpart in the reference) -----
+ * For callers that cannot call cudaMalloc -- an application whose device
+ * memory belongs to another allocator, or a service that must not allocate
+ * after start-up.  Same job and results as fpl_run_async on device buffers,
+ * on the current CUDA device, but no context is needed and nothing is
+ * allocated: the kernels' scratch is a fixed array inside the library, held
+ * by every GPU that loads it until the process exits.  The first call on a
+ * device looks up that array's device address; make that first call before
+ * any stream capture.  A call covers at most FPL_NOALLOC_MAX_PIXELS pixels
+ * ((row_end - row_begin) * cols); larger jobs return FPL_ERR_NOALLOC_LIMIT and
+ * can be split into row ranges.  All calls share the array, so calls whose
+ * work overlaps on the GPU race; serialise them on one stream. */
+#define FPL_NOALLOC_MAX_PIXELS 524288
+int fpl_run_noalloc(const fpl_job *job, void *stream);
 
 /* ---- diagnostics (no counterpart in the reference) ------------------------ */
 /* Text of the last CUDA / device error seen by the context. */
