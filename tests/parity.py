@@ -50,3 +50,51 @@ def assert_parity(m, phase_tol=PHASE_RMS_TOL, tcorr_tol=TCORR_TOL, max_code_mism
     assert m["phase_rms"] <= phase_tol, m
     assert m["tcorr_max"] <= tcorr_tol, m
     assert m["zero_mismatch"] == 0, m
+
+
+GOLDEN = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.abspath(__file__)),
+                                    "golden", "golden_phase_link.npz")
+
+
+def load_golden():
+    """Golden vectors made by tests/golden/make_golden.py from the reference's
+    own EVWorker + LAPACK.  Returns {case: {"stack", "nmap", "ny", "nx",
+    "variants": {key: (method, semantics, extra, result)}}}."""
+    d = np.load(GOLDEN)
+    cases = {}
+    for name in d.files:
+        if name.endswith("/shape"):
+            case = name.split("/")[0]
+            R, C, N, ny, nx = [int(x) for x in d[name]]
+            cases[case] = {"stack": d[case + "/stack"], "nmap": d[case + "/nmap"],
+                           "ny": ny, "nx": nx, "variants": {}}
+    for name in d.files:
+        if not name.endswith("/tcorr"):
+            continue
+        case, var = name.split("/")[:2]
+        parts = var.split("_")
+        method, sem = parts[0], parts[1]
+        if sem == "phase":                    # "phase_link"
+            sem = "phase_link"
+        extra = {}
+        # extras are encoded as _<name><value>
+        tail = var[len(method) + 1 + len(sem):]
+        for key in ("band_width", "min_neighbors", "mini_stack_count"):
+            tag = "_" + key
+            if tag in tail:
+                val = tail.split(tag, 1)[1]
+                num = ""
+                for ch in val:
+                    if ch.isdigit():
+                        num += ch
+                    else:
+                        break
+                extra[key] = int(num)
+        k = case + "/" + var
+        ang = d[k + "/phase_angle"]
+        zero = d[k + "/phase_zero"]
+        phase = np.exp(1j * ang.astype(np.float64)).astype(np.complex64)
+        phase[:, zero] = 0
+        res = {"phase": phase, "tcorr": d[k + "/tcorr"], "comp": d[k + "/comp"]}
+        cases[case]["variants"][var] = (method, sem, extra, res)
+    return cases

@@ -10,7 +10,7 @@ import pytest
 
 import oracle
 from fringe_gb300 import synth
-from tests.parity import assert_parity, compare
+from tests.parity import assert_parity, compare, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -139,3 +139,16 @@ def test_row_range_and_torch_device_path(gpu_lib, vor30):
     assert np.array_equal(dev["phase"].cpu().numpy(), full["phase"])
     assert np.array_equal(dev["tcorr"].cpu().numpy(), full["tcorr"])
     assert np.array_equal(dev["comp"].cpu().numpy(), full["comp"])
+
+
+def test_golden_vectors_from_the_reference(gpu_lib):
+    """GPU results against golden vectors made with the reference's own
+    EVWorker + LAPACK (tests/golden/make_golden.py)."""
+    from fringe_gb300 import phase_link
+    for case, g in load_golden().items():
+        for var, (method, sem, extra, ref) in g["variants"].items():
+            got = phase_link(g["stack"], g["nmap"], (g["ny"], g["nx"]), method=method,
+                             semantics=sem, **extra)
+            m = compare(got, ref)
+            assert m["valid_both"] > 0, (case, var, m)
+            assert_parity(m)
