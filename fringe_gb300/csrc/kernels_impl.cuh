@@ -39,7 +39,7 @@ static cudaError_t launch_t(const KParams &P, int num_sms, cudaStream_t st)
     const size_t per_warp = Lay<T, NP>::bytes;
     const size_t budget = 224 * 1024;   // of the 227 KB a block may opt into
     int warps = int(budget / per_warp);
-    if (warps > 8) warps = 8;
+    if (warps > 16) warps = 16;
     if (warps < 1) warps = 1;
     const size_t smem = per_warp * warps;
     int dev = 0;
