@@ -8,6 +8,7 @@
 // stream.  No host round trip separates the two passes.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -70,7 +71,6 @@ int fpl_validate_job(const fpl_job *job)
         if (job->band_width <= 0 || job->band_width >= job->nbands - 1) return FPL_ERR_OPTIONS;
     }
     if (job->precision != FPL_PREC_FP32 && job->precision != FPL_PREC_MIXED) return FPL_ERR_OPTIONS;
-    if (job->precision == FPL_PREC_MIXED) return FPL_ERR_UNSUPPORTED;   // tensor-core form not built yet
     if (job->memory != FPL_MEM_HOST && job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
     int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
     if (r0 < 0 || r0 > r1 || r1 > job->rows) return FPL_ERR_OPTIONS;
@@ -143,7 +143,7 @@ int fpl_ctx_destroy(fpl_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
     void *bufs[] = {ctx->d_stack, ctx->d_nmap, ctx->d_phase, ctx->d_tcorr, ctx->d_comp,
-                    ctx->d_status, ctx->d_fb_list, ctx->d_small};
+                    ctx->d_status, ctx->d_fb_list, ctx->d_small, ctx->d_cbuf, ctx->d_cinfo};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -169,6 +169,7 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
                 bool fp64_all)
 {
     const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
+    int rc = 0;
     KParams P;
     std::memset(&P, 0, sizeof(P));
     P.stack = static_cast<const float2 *>(stack);
@@ -202,7 +203,7 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
     P.slow = reinterpret_cast<int *>(static_cast<char *>(ctx->d_small) + 32);
     // work list: at most one entry per pixel of the range
     size_t need = sizeof(long long) * (size_t)(P.npix > 0 ? P.npix : 1);
-    int rc = grow(ctx, &ctx->d_fb_list, &ctx->cap_fb_list, need);
+    rc = grow(ctx, &ctx->d_fb_list, &ctx->cap_fb_list, need);
     if (rc) return rc;
     P.fb_list = static_cast<long long *>(ctx->d_fb_list);
     P.fb_cap = (int)(P.npix < 0x7fffffff ? P.npix : 0x7fffffff);
@@ -224,7 +225,31 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
         ev = &ctx->prof_ev[3 * ctx->prof_used++];
         FPL_CUDA(ctx, cudaEventRecord(ev[0], st));
     }
-    FPL_CUDA(ctx, fpl::launch_fp32(P, ctx->num_sms, st));
+    const bool mixed = job->precision == FPL_PREC_MIXED && P.nb <= 32 && P.K <= 1024;
+    if (mixed) {
+        // tensor-core coherence matrices, then eigen-solves, chunk by chunk
+        // of rows so the packed matrices stay within a bounded buffer
+        const int npk = P.nb * (P.nb + 1) / 2;
+        const long long chunk_px_max = std::max<long long>(P.cols, (1ll << 20));
+        const int rows_per_chunk = (int)std::max<long long>(1, chunk_px_max / P.cols);
+        const long long chunk_px = (long long)std::min(rows_per_chunk, r1 - r0) * P.cols;
+        if ((rc = grow(ctx, &ctx->d_cbuf, &ctx->cap_cbuf, sizeof(float2) * (size_t)npk * chunk_px))) return rc;
+        if ((rc = grow(ctx, &ctx->d_cinfo, &ctx->cap_cinfo, sizeof(int) * (size_t)chunk_px))) return rc;
+        for (int ra = r0; ra < r1; ra += rows_per_chunk) {
+            const int rb = std::min(r1, ra + rows_per_chunk);
+            KParams Q = P;
+            Q.pix_begin = (long long)ra * P.cols;
+            Q.npix = (long long)(rb - ra) * P.cols;
+            Q.cbuf = static_cast<float2 *>(ctx->d_cbuf);
+            Q.cinfo = static_cast<int *>(ctx->d_cinfo);
+            Q.cbase = Q.pix_begin;
+            Q.cstride = npk;
+            FPL_CUDA(ctx, fpl::launch_gram_tc(Q, ctx->num_sms, st));
+            FPL_CUDA(ctx, fpl::launch_solve(Q, ctx->num_sms, st));
+        }
+    } else {
+        FPL_CUDA(ctx, fpl::launch_fp32(P, ctx->num_sms, st));
+    }
     if (ev) FPL_CUDA(ctx, cudaEventRecord(ev[1], st));
     FPL_CUDA(ctx, fpl::launch_fp64(P, ctx->num_sms, st));
     if (ev) FPL_CUDA(ctx, cudaEventRecord(ev[2], st));

@@ -26,6 +26,9 @@ struct fpl_ctx {
     void *d_fb_list = nullptr;
     size_t cap_fb_list = 0;
     void *d_small = nullptr;
+    // mixed form: packed coherence matrices of one chunk of rows
+    void *d_cbuf = nullptr, *d_cinfo = nullptr;
+    size_t cap_cbuf = 0, cap_cinfo = 0;
     // tuning
     float amb_scale = kDefaultAmbScale;
     float cond_max = kDefaultCondMax;

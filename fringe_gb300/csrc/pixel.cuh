@@ -49,7 +49,14 @@ struct KParams {
     int fb_cap;
     unsigned *err;                      // error flags (scratch)
     int *slow;                          // pixels that left the fast eigen path (scratch)
+    // mixed form: packed coherence matrices from the tensor-core kernel
+    float2 *cbuf;                       // [pixel - cbase][n(n+1)/2], rows of the upper triangle
+    int *cinfo;                         // [pixel - cbase]: SHP count, or CI_* below
+    long long cbase;                    // first pixel of the buffers
+    int cstride;                        // n(n+1)/2
 };
+
+enum { CI_CENTRE = -1, CI_FEW = -2, CI_BAD = -3 };
 
 enum { M_MLE = 0, M_EVD = 1, M_STBAS = 2 };
 enum { SEM_EVD = 0, SEM_PL = 1 };
@@ -803,8 +810,11 @@ __device__ __forceinline__ void put_code(const KParams &P, long long pp, int lan
     }
 }
 
+// Gather, Gamma and coherence (evd.cpp:514-582).  Returns the SHP count
+// with C in the warp's slab, or -1 when the pixel is finished (skipped or
+// coded) and its outputs are written.
 template <typename T, int NP>
-__device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm, int lane)
+__device__ int pixel_coherence(const KParams &P, long long pp, unsigned char *sm, int lane)
 {
     using L = Lay<T, NP>;
     constexpr int LD = L::LD;
@@ -839,7 +849,7 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
     const bool centre = (__ldg(cen + (cflat >> 5)) >> (cflat & 31)) & 1u;
     if (!centre) {                                           // evd.cpp:517
         if (P.status && lane == 0) P.status[pp] = 1;
-        return;
+        return -1;
     }
 
     // ---- block ownership for the Gamma accumulation ----------------------
@@ -949,7 +959,7 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
     const int min_neigh = plink ? P.min_neigh : 2;            // evd.cpp:566 / phase_link.cpp:524
     if (npix < min_neigh) {
         if (P.status && lane == 0) P.status[pp] = 2;
-        return;
+        return -1;
     }
 
     // ---- coherence (evd.cpp:569-582) -------------------------------------
@@ -991,9 +1001,29 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
             // non-finite coherence: LAPACK's answer on NaN input is undefined;
             // the first eigen call is reported as failed.
             put_code(P, pp, lane, (!plink && P.method != M_MLE) ? -6 : -1);
-            return;
+            return -1;
         }
     }
+    return npix;
+}
+
+
+// Eigen-solve and outputs for a pixel whose coherence C is in the warp's
+// slab (evd.cpp:584-786, phase_link.cpp:540-665).
+template <typename T, int NP>
+__device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, int lane, int npix)
+{
+    using L = Lay<T, NP>;
+    constexpr int LD = L::LD;
+    C2<T> *Cm = reinterpret_cast<C2<T> *>(sm + L::cm);
+    C2<T> *Wm = reinterpret_cast<C2<T> *>(sm + L::wm);
+    T *Xr = reinterpret_cast<T *>(sm + L::xr);
+    T *yv = reinterpret_cast<T *>(sm + L::yy);
+    C2<T> *col = reinterpret_cast<C2<T> *>(sm + L::vv);
+    float2 *phs = reinterpret_cast<float2 *>(sm + L::ph);
+    const int n = P.nb;
+    const long long plane = P.plane;
+    const bool plink = (P.semantics == SEM_PL);
 
     const bool fp32 = sizeof(T) == 4;
     const T amb = T(P.amb) * T(n) * Eps<T>::v;          // rounding band unit (FP32 only)
@@ -1280,6 +1310,55 @@ __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm,
             if (P.status) P.status[pp] = pstatus;
         }
     }
+}
+
+
+// Mixed form: the coherence C of pixel pp was formed on the tensor cores
+// (gram_tc.cu) and stored as the packed upper triangle; load it into the
+// warp's slab.  Returns the SHP count, or -1 when the pixel is finished.
+template <int NP>
+__device__ int pixel_load_coherence(const KParams &P, long long pp, unsigned char *sm, int lane)
+{
+    using L = Lay<float, NP>;
+    constexpr int LD = L::LD;
+    C2<float> *Cm = reinterpret_cast<C2<float> *>(sm + L::cm);
+    const int n = P.nb;
+    const long long plane = P.plane;
+    for (int b = lane; b < n; b += 32) P.phase[b * plane + pp] = make_float2(0.f, 0.f);
+    if (lane == 0) {
+        P.tcorr[pp] = 0.f;
+        P.comp[pp] = make_float2(0.f, 0.f);
+    }
+    const long long loc = pp - P.cbase;
+    const int info = P.cinfo[loc];
+    if (info == CI_CENTRE || info == CI_FEW) {
+        if (P.status && lane == 0) P.status[pp] = (info == CI_CENTRE) ? 1 : 2;
+        return -1;
+    }
+    if (info == CI_BAD) {
+        const bool plink = (P.semantics == SEM_PL);
+        put_code(P, pp, lane, (!plink && P.method != M_MLE) ? -6 : -1);
+        return -1;
+    }
+    const float2 *src = P.cbuf + loc * P.cstride;
+    int off = 0;
+    for (int i = 0; i < n; ++i) {
+        for (int j = i + lane; j < n; j += 32) {
+            const float2 v = src[off + (j - i)];
+            Cm[i * LD + j] = cmk<float>(v.x, v.y);
+            Cm[j * LD + i] = cmk<float>(v.x, -v.y);
+        }
+        off += n - i;
+    }
+    __syncwarp();
+    return info;
+}
+
+template <typename T, int NP>
+__device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm, int lane)
+{
+    const int npix = pixel_coherence<T, NP>(P, pp, sm, lane);
+    if (npix >= 0) pixel_solve<T, NP>(P, pp, sm, lane, npix);
 }
 
 }  // namespace fpl
