@@ -31,16 +31,18 @@ namespace fpl {
 namespace {
 
 constexpr int TC_THREADS = 128;
-constexpr int TC_KC = 256;                        // samples per MMA chunk
+constexpr int TC_KC = 128;                        // samples per MMA chunk
 constexpr int TC_ROWS = 128;                      // [Re hi; Im hi; Re lo; Im lo] x 32 dates
 constexpr int TC_SBO = TC_KC * 16;                // bytes between 8-row groups
-constexpr int TC_A_BYTES = TC_ROWS * TC_KC * 2;   // 64 KiB
+constexpr int TC_A_BYTES = TC_ROWS * TC_KC * 2;   // 32 KiB
 constexpr int TC_LDD = 65;                        // D staging row stride (floats)
 constexpr int TC_D_BYTES = TC_ROWS * TC_LDD * 4;
 constexpr int TC_MAXK = 1024;                     // window taps (nulong <= 32)
-constexpr int TC_TMEM_COLS = 128;                 // allocation (power of two >= 64 used)
-constexpr size_t TC_OFF_D = TC_A_BYTES;
-constexpr size_t TC_OFF_SHP = TC_OFF_D + TC_D_BYTES;
+constexpr int TC_TMEM_COLS = 64;                  // the N = 64 accumulator
+// D is staged in the operand buffer, which is free once the MMAs complete
+constexpr size_t TC_OFF_D = 0;
+constexpr size_t TC_AD_BYTES = (TC_A_BYTES > TC_D_BYTES ? TC_A_BYTES : TC_D_BYTES);
+constexpr size_t TC_OFF_SHP = (TC_AD_BYTES + 127) & ~size_t(127);
 constexpr size_t TC_OFF_MISC = TC_OFF_SHP + TC_MAXK * 4;
 constexpr size_t TC_SMEM = TC_OFF_MISC + 256;
 constexpr unsigned ERR_TC_TIMEOUT = 2u;
@@ -209,8 +211,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_gram_tc(KParams P)
             const int len = min(TC_KC, npix - c0);
             const int kpad = (len + 15) & ~15;
             const int ncc = kpad >> 3;                         // 8-sample column chunks
+            // task = (date d, 8-sample chunk ck): consecutive threads take
+            // consecutive dates, so a warp's 16-byte stores fill whole
+            // 128-byte core-matrix rows (no bank conflicts)
+#pragma unroll 2
             for (int t = tid; t < 32 * ncc; t += TC_THREADS) {
-                const int d = t / ncc, ck = t - d * ncc;
+                const int d = t & 31, ck = t >> 5;
                 float re[8], im[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
@@ -291,27 +297,26 @@ __global__ void __launch_bounds__(TC_THREADS) k_gram_tc(KParams P)
             if (tid == 0) flag[0] = bad ? 1 : 0;
         }
         __syncthreads();
-        bool badc = flag[0] != 0;
+        const bool badc = flag[0] != 0;
         if (!badc) {
+            // row i of the packed upper triangle starts at i n - i(i-1)/2;
+            // warps take rows, lanes take columns j >= i (conflict-free reads)
             float2 *dst = P.cbuf + loc * P.cstride;
-            for (int e = tid; e < npk; e += TC_THREADS) {
-                // row i of the packed upper triangle: e = i n - i(i-1)/2 + (j - i)
-                int i = (int)((2.f * n + 1.f - sqrtf((2.f * n + 1.f) * (2.f * n + 1.f) - 8.f * e)) * 0.5f);
-                if (i < 0) i = 0;
-                while (i > 0 && i * n - i * (i - 1) / 2 > e) --i;
-                while ((i + 1) * n - (i + 1) * i / 2 <= e) ++i;
-                const int j = i + (e - (i * n - i * (i - 1) / 2));
-                float2 c;
-                if (i == j) {
-                    c = make_float2(1.f, 0.f);
-                } else {
-                    const float re = S(i, j) + S(32 + i, 32 + j);
-                    const float im = S(32 + i, j) - S(i, 32 + j);
-                    const float sc = rs[i] * rs[j];
-                    c = make_float2(re * sc, im * sc);
-                    if (!isfinite(c.x) || !isfinite(c.y)) flag[0] = 1;
+            for (int i = warp; i < n; i += 4) {
+                const int off = i * n - i * (i - 1) / 2;
+                for (int j = i + lane; j < n; j += 32) {
+                    float2 c;
+                    if (i == j) {
+                        c = make_float2(1.f, 0.f);
+                    } else {
+                        const float re = S(i, j) + S(32 + i, 32 + j);
+                        const float im = S(32 + i, j) - S(i, 32 + j);
+                        const float sc = rs[i] * rs[j];
+                        c = make_float2(re * sc, im * sc);
+                        if (!isfinite(c.x) || !isfinite(c.y)) flag[0] = 1;
+                    }
+                    dst[off + (j - i)] = c;
                 }
-                dst[e] = c;
             }
         }
         __syncthreads();
@@ -344,13 +349,15 @@ cudaError_t launch_gram_tc(const KParams &P, int num_sms, cudaStream_t st)
     if (dev < 64 && !configured[dev]) {
         cudaError_t e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
         if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        if (e != cudaSuccess) return e;
         configured[dev] = true;
     }
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gram_tc, TC_THREADS, TC_SMEM);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
-    if (per_sm > 2) per_sm = 2;               // 2 x 128 TMEM columns of the 512
+    if (per_sm > 8) per_sm = 8;               // 8 x 64 TMEM columns of the 512
     long long blocks = (long long)num_sms * per_sm;
     if (P.npix < blocks) blocks = P.npix > 0 ? P.npix : 1;
     k_gram_tc<<<(unsigned)blocks, TC_THREADS, TC_SMEM, st>>>(P);

@@ -64,6 +64,8 @@ static cudaError_t launch_solve_t(const KParams &P, int num_sms, cudaStream_t st
     if (dev < 64 && !configured[dev]) {
         cudaError_t e = cudaFuncSetAttribute(k_solve<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(k_solve<NP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        if (e != cudaSuccess) return e;
         configured[dev] = true;
     }
     int per_sm = 0;
@@ -91,6 +93,8 @@ static cudaError_t launch_t(const KParams &P, int num_sms, cudaStream_t st)
     cudaGetDevice(&dev);
     if (dev < 64 && !configured[dev]) {
         cudaError_t e = cudaFuncSetAttribute(k_pixels<T, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(k_pixels<T, NP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (e != cudaSuccess) return e;
         configured[dev] = true;
     }

@@ -170,26 +170,29 @@ __device__ bool warp_chol_c(C2<T> *A, int n, C2<T> *col, int lane)
         for (int i = j + 1 + lane; i < n; i += 32) {
             const C2<T> li = col[i];
             C2<T> *__restrict__ Ai = A + i * LD;
-            // A[i][k] -= l_i conj(l_k), k in (j, i]; col[k] = 0 for k <= j
-            const int k0 = (j + 1) & ~1;
-#pragma unroll 2
-            for (int k = k0; k <= i; k += 2) {
-                C2<T> l0, l1;
+            // A[i][k] -= l_i conj(l_k), k in (j, i]; col[k] = 0 for k <= j.
+            // Four columns per step, loads issued before the stores.
+            for (int k = (j + 1) & ~3; k <= i; k += 4) {
+                C2<T> l[4], a[4];
                 if (sizeof(T) == 4) {
-                    const float4 v = *reinterpret_cast<const float4 *>(col + k);
-                    l0 = cmk<T>(T(v.x), T(v.y));
-                    l1 = cmk<T>(T(v.z), T(v.w));
+                    const float4 v0 = *reinterpret_cast<const float4 *>(col + k);
+                    const float4 v1 = *reinterpret_cast<const float4 *>(col + k + 2);
+                    l[0] = cmk<T>(T(v0.x), T(v0.y)); l[1] = cmk<T>(T(v0.z), T(v0.w));
+                    l[2] = cmk<T>(T(v1.x), T(v1.y)); l[3] = cmk<T>(T(v1.z), T(v1.w));
                 } else {
-                    l0 = col[k];
-                    l1 = col[k + 1];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) l[u] = col[k + u];
                 }
-                C2<T> a0 = Ai[k], a1 = Ai[k + 1];
-                a0.x -= li.x * l0.x + li.y * l0.y;
-                a0.y -= li.y * l0.x - li.x * l0.y;
-                a1.x -= li.x * l1.x + li.y * l1.y;
-                a1.y -= li.y * l1.x - li.x * l1.y;
-                if (k > j) Ai[k] = a0;
-                if (k + 1 <= i) Ai[k + 1] = a1;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) a[u] = Ai[k + u];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    a[u].x -= li.x * l[u].x + li.y * l[u].y;
+                    a[u].y -= li.y * l[u].x - li.x * l[u].y;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (k + u > j && k + u <= i) Ai[k + u] = a[u];
             }
         }
         __syncwarp();
@@ -277,19 +280,21 @@ __device__ bool warp_sweep_inverse(T *A, int n, T *rowk, T *inf_norm, int lane)
             const T a = own ? T(0) : T(1);
             const T b = own ? rp : -f;
             int j = 0;
-            for (; j + 4 <= n; j += 4) {
-                T r0, r1, r2, r3;
+            for (; j + 8 <= n; j += 8) {
+                T r[8], x[8];
                 if (sizeof(T) == 4) {
-                    const float4 r4 = *reinterpret_cast<const float4 *>(rowk + j);
-                    r0 = T(r4.x); r1 = T(r4.y); r2 = T(r4.z); r3 = T(r4.w);
+                    const float4 v0 = *reinterpret_cast<const float4 *>(rowk + j);
+                    const float4 v1 = *reinterpret_cast<const float4 *>(rowk + j + 4);
+                    r[0] = T(v0.x); r[1] = T(v0.y); r[2] = T(v0.z); r[3] = T(v0.w);
+                    r[4] = T(v1.x); r[5] = T(v1.y); r[6] = T(v1.z); r[7] = T(v1.w);
                 } else {
-                    r0 = rowk[j]; r1 = rowk[j + 1]; r2 = rowk[j + 2]; r3 = rowk[j + 3];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) r[u] = rowk[j + u];
                 }
-                const T x0 = Ai[j], x1 = Ai[j + 1], x2 = Ai[j + 2], x3 = Ai[j + 3];
-                Ai[j] = fma(b, r0, a * x0);
-                Ai[j + 1] = fma(b, r1, a * x1);
-                Ai[j + 2] = fma(b, r2, a * x2);
-                Ai[j + 3] = fma(b, r3, a * x3);
+#pragma unroll
+                for (int u = 0; u < 8; ++u) x[u] = Ai[j + u];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) Ai[j + u] = fma(b, r[u], a * x[u]);
             }
             for (; j < n; ++j) Ai[j] = fma(b, rowk[j], a * Ai[j]);
             Ai[k] = own ? -rp : f;
