@@ -14,6 +14,7 @@ FPL_METHOD = {"MLE": 0, "EVD": 1, "STBAS": 2}
 FPL_SEMANTICS = {"evd": 0, "phase_link": 1}
 FPL_PRECISION = {"fp32": 0, "mixed": 1}
 FPL_MEM_HOST, FPL_MEM_DEVICE = 0, 1
+FPL_BATCH_GRAPH, FPL_BATCH_AUTOTUNE = 1, 2
 
 
 class FplJob(ctypes.Structure):
@@ -60,6 +61,11 @@ _SIGS = {
     "fpl_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "fpl_version": (ctypes.c_char_p, []),
     "fpl_run_noalloc": (ctypes.c_int, [ctypes.POINTER(FplJob), _P]),
+    "fpl_batch_create": (ctypes.c_int, [_P, ctypes.POINTER(FplJob), ctypes.c_int, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "fpl_batch_run": (ctypes.c_int, [_P, _P]),
+    "fpl_batch_stats": (ctypes.c_int, [_P, ctypes.POINTER(FplStats)]),
+    "fpl_batch_destroy": (ctypes.c_int, [_P]),
     "fpl_ctx_set_tuning": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
     "fpl_ctx_last_error": (ctypes.c_char_p, [_P]),
     "fpl_ctx_set_profiling": (ctypes.c_int, [_P, ctypes.c_int]),

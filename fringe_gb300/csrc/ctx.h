@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -38,6 +39,8 @@ struct fpl_ctx {
     std::vector<cudaEvent_t> prof_ev;   // 3 per run: before FP32, between, after FP64
     size_t prof_used = 0;
     fpl_stats stats = {};
+    // autotuned warps per CTA of batch launches, keyed by (depth, taps, SHP density)
+    std::map<long long, int> tuned_warps;
     std::string last_error;
 };
 

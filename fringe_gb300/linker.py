@@ -89,3 +89,63 @@ def _run_torch(lib, ctx, stack, nmap, ny, nx, method, semantics, mini, bw, minn,
     _lib.check(lib.fpl_run_async(ctx.handle, ctypes.byref(job), ctypes.c_void_p(stream)),
                ctx.handle)
     return out
+
+
+class PhaseLinkBatch:
+    """Many CUDA-tensor jobs in one persistent launch (fpl_batch_*).
+
+    ``jobs`` is a list of dicts with keys stack, nmap (CUDA tensors),
+    half_window, and optionally method, semantics, mini_stack_count,
+    band_width, min_neighbors.  Outputs are allocated once; ``run()`` fills
+    them (replaying a captured CUDA graph when ``graph=True``).
+    """
+
+    def __init__(self, jobs, graph=True, autotune=False, device=0, ctx=None):
+        import torch
+        self.ctx = ctx or _lib.context(device)
+        self.lib = _lib.load()
+        self.outputs = []
+        self._keep = []
+        arr = (_lib.FplJob * len(jobs))()
+        for k, j in enumerate(jobs):
+            stack = j["stack"].contiguous()
+            nmap = j["nmap"].contiguous()
+            nb, R, C = stack.shape
+            ny, nx = j["half_window"]
+            out = {"phase": torch.zeros((nb, R, C), dtype=torch.complex64, device=stack.device),
+                   "tcorr": torch.zeros((R, C), dtype=torch.float32, device=stack.device),
+                   "comp": torch.zeros((R, C), dtype=torch.complex64, device=stack.device)}
+            self.outputs.append(out)
+            self._keep += [stack, nmap]
+            arr[k] = _make_job(nb, R, C, ny, nx, j.get("method", "MLE"), j.get("semantics", "evd"),
+                               j.get("mini_stack_count", 1), j.get("band_width", -1),
+                               j.get("min_neighbors", 2), "fp32", j.get("rows"), _lib.FPL_MEM_DEVICE,
+                               stack.data_ptr(), nmap.data_ptr(), out["phase"].data_ptr(),
+                               out["tcorr"].data_ptr(), out["comp"].data_ptr(), None)
+        flags = (_lib.FPL_BATCH_GRAPH if graph else 0) | (_lib.FPL_BATCH_AUTOTUNE if autotune else 0)
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.fpl_batch_create(self.ctx.handle, arr, len(jobs), flags, ctypes.byref(h)),
+                   self.ctx.handle)
+        self.handle = h
+
+    def run(self, stream=None):
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _lib.check(self.lib.fpl_batch_run(self.handle, ctypes.c_void_p(s)), self.ctx.handle)
+        return self.outputs
+
+    def stats(self):
+        st = _lib.FplStats()
+        _lib.check(self.lib.fpl_batch_stats(self.handle, ctypes.byref(st)), self.ctx.handle)
+        return {k: getattr(st, k) for k, _ in _lib.FplStats._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.fpl_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -148,6 +148,26 @@ int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream);
 
 int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out);
 
+/* ---- batches of jobs ------------------------------------------------------
+ * Many device-memory jobs -- scenes or ministacks of different size, stack
+ * depth, window and method -- run as one persistent launch per padded depth
+ * (16 / 32 / 64 dates), with warps taking pixels dynamically across jobs,
+ * followed by one FP64 settle launch.  Replaces running the evd module once
+ * per ministack (src/sequential/sequential.py:193-254 calls evd_process in a
+ * loop).  FPL_BATCH_GRAPH captures the launch sequence into a CUDA graph at
+ * creation; fpl_batch_run replays it (buffers are fixed, their contents may
+ * change between runs).  FPL_BATCH_AUTOTUNE times candidate CTA shapes on
+ * the batch at creation and caches the fastest per (depth, window, mean SHP
+ * count) in the context.  Batches use the plain FP32 form. */
+#define FPL_BATCH_GRAPH 1
+#define FPL_BATCH_AUTOTUNE 2
+typedef struct fpl_batch fpl_batch;
+int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fpl_batch **out);
+int fpl_batch_run(fpl_batch *batch, void *stream);
+/* waits for the device; fp64_pixels / slow_path_pixels summed over the jobs */
+int fpl_batch_stats(const fpl_batch *batch, fpl_stats *out);
+int fpl_batch_destroy(fpl_batch *batch);
+
 /* ---- run without device allocation (no counterpart in the reference) -----
  * For callers that cannot call cudaMalloc -- an application whose device
  * memory belongs to another allocator, or a service that must not allocate
