@@ -36,6 +36,16 @@ class FplStats(ctypes.Structure):
                 ("kernel_ms", ctypes.c_float), ("total_ms", ctypes.c_float)]
 
 
+class FplServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget", ctypes.c_size_t), ("wave_pixels", ctypes.c_longlong),
+                ("device", ctypes.c_int)]
+
+
+class FplTicketInfo(ctypes.Structure):
+    _fields_ = [("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double), ("rc", ctypes.c_int)]
+
+
 class FplOptions(ctypes.Structure):
     _fields_ = [
         ("inputDS", ctypes.c_char_p), ("wtsDS", ctypes.c_char_p),
@@ -66,6 +76,12 @@ _SIGS = {
     "fpl_batch_run": (ctypes.c_int, [_P, _P]),
     "fpl_batch_stats": (ctypes.c_int, [_P, ctypes.POINTER(FplStats)]),
     "fpl_batch_destroy": (ctypes.c_int, [_P]),
+    "fpl_server_config_default": (None, [ctypes.POINTER(FplServerConfig)]),
+    "fpl_server_create": (ctypes.c_int, [ctypes.POINTER(FplServerConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "fpl_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(FplJob), ctypes.POINTER(ctypes.c_ulonglong)]),
+    "fpl_server_wait": (ctypes.c_int, [_P, ctypes.c_ulonglong, ctypes.c_double,
+                                       ctypes.POINTER(FplTicketInfo)]),
+    "fpl_server_destroy": (ctypes.c_int, [_P]),
     "fpl_ctx_set_tuning": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
     "fpl_ctx_last_error": (ctypes.c_char_p, [_P]),
     "fpl_ctx_set_profiling": (ctypes.c_int, [_P, ctypes.c_int]),

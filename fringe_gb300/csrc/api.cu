@@ -108,6 +108,7 @@ const char *fpl_error_string(int code)
     case FPL_ERR_UNSUPPORTED: return "unsupported size (nbands > 64 or window > 1024 taps)";
     case FPL_ERR_DEVICE_CHECK: return "a kernel reported an internal error";
     case FPL_ERR_NULL: return "a required pointer is NULL";
+    case FPL_ERR_TIMEOUT: return "timed out waiting for a served job";
     case FPL_ERR_NOALLOC_LIMIT: return "job exceeds the FPL_NOALLOC_MAX_PIXELS scratch of fpl_run_noalloc";
     }
     return "unknown error";

@@ -20,17 +20,13 @@
 #include <map>
 #include <vector>
 
+#include "batch.h"
 #include "ctx.h"
 #include "fringe_gb300.h"
 #include "kernels.h"
 #include "pixel.cuh"
 
 namespace fpl {
-
-struct BatchEntry {
-    KParams P;
-    long long px_offset;   // first pixel of this job in the class's concatenated range
-};
 
 constexpr int kBatchChunk = 2;   // pixels a warp takes per counter increment
 
@@ -88,7 +84,6 @@ __global__ void k_popcount(const uint32_t *__restrict__ w, long long nwords, uns
 }
 
 namespace {
-
 template <typename KernelFn>
 cudaError_t configure(KernelFn k, size_t smem)
 {
@@ -111,6 +106,8 @@ size_t warp_bytes(int np, bool fp64)
     }
     return 0;
 }
+
+}  // namespace
 
 int max_warps(int np, bool fp64)
 {
@@ -186,7 +183,35 @@ cudaError_t launch_batch64(int np, const BatchEntry *jobs, int njobs, int num_sm
     return cudaErrorInvalidValue;
 }
 
-}  // namespace
+void fill_params(KParams &P, const fpl_job &jb, int r0, int r1, float amb, float cond_max)
+{
+    std::memset(&P, 0, sizeof(P));
+    P.stack = static_cast<const float2 *>(jb.stack);
+    P.nmap = jb.nmap;
+    P.phase = static_cast<float2 *>(jb.phase);
+    P.tcorr = jb.tcorr;
+    P.comp = static_cast<float2 *>(jb.comp);
+    P.status = jb.status;
+    P.rows = jb.rows;
+    P.cols = jb.cols;
+    P.nb = jb.nbands;
+    P.ny = jb.half_window_y;
+    P.nx = jb.half_window_x;
+    P.wx = 2 * jb.half_window_x + 1;
+    P.K = (2 * jb.half_window_y + 1) * P.wx;
+    P.nulong = (P.K + 31) / 32;
+    P.plane = (long long)jb.rows * jb.cols;
+    P.pix_begin = (long long)r0 * jb.cols;
+    P.npix = (long long)(r1 - r0) * jb.cols;
+    P.method = jb.method;
+    P.semantics = jb.semantics;
+    P.mini = jb.mini_stack_count;
+    P.bw = jb.band_width;
+    P.min_neigh = jb.min_neighbors;
+    P.amb = amb;
+    P.cond_max = cond_max;
+}
+
 }  // namespace fpl
 
 // ---------------------------------------------------------------------------
@@ -290,31 +315,7 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
         const fpl_job &jb = jobs[j];
         const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
         fpl::KParams &P = table[e].P;
-        std::memset(&P, 0, sizeof(P));
-        P.stack = static_cast<const float2 *>(jb.stack);
-        P.nmap = jb.nmap;
-        P.phase = static_cast<float2 *>(jb.phase);
-        P.tcorr = jb.tcorr;
-        P.comp = static_cast<float2 *>(jb.comp);
-        P.status = jb.status;
-        P.rows = jb.rows;
-        P.cols = jb.cols;
-        P.nb = jb.nbands;
-        P.ny = jb.half_window_y;
-        P.nx = jb.half_window_x;
-        P.wx = 2 * jb.half_window_x + 1;
-        P.K = (2 * jb.half_window_y + 1) * P.wx;
-        P.nulong = (P.K + 31) / 32;
-        P.plane = (long long)jb.rows * jb.cols;
-        P.pix_begin = (long long)r0 * jb.cols;
-        P.npix = (long long)(r1 - r0) * jb.cols;
-        P.method = jb.method;
-        P.semantics = jb.semantics;
-        P.mini = jb.mini_stack_count;
-        P.bw = jb.band_width;
-        P.min_neigh = jb.min_neighbors;
-        P.amb = ctx->amb_scale;
-        P.cond_max = ctx->cond_max;
+        fpl::fill_params(P, jb, r0, r1, ctx->amb_scale, ctx->cond_max);
         P.fb_count = reinterpret_cast<int *>(cnt_base + kJobCounterBytes * e);
         P.err = reinterpret_cast<unsigned *>(cnt_base + kJobCounterBytes * e + 16);
         P.slow = reinterpret_cast<int *>(cnt_base + kJobCounterBytes * e + 32);

@@ -87,6 +87,7 @@ enum fpl_pixel_status {
 #define FPL_ERR_DEVICE_CHECK   204   /* a kernel reported an internal error */
 #define FPL_ERR_NULL           205   /* a required pointer is NULL */
 #define FPL_ERR_NOALLOC_LIMIT  206   /* job larger than fpl_run_noalloc's scratch */
+#define FPL_ERR_TIMEOUT        207   /* fpl_server_wait gave up */
 
 #define FPL_MAX_BANDS 64
 #define FPL_MAX_NULONG 32
@@ -167,6 +168,35 @@ int fpl_batch_run(fpl_batch *batch, void *stream);
 /* waits for the device; fp64_pixels / slow_path_pixels summed over the jobs */
 int fpl_batch_stats(const fpl_batch *batch, fpl_stats *out);
 int fpl_batch_destroy(fpl_batch *batch);
+
+/* ---- serving loop -----------------------------------------------------------
+ * A request loop for phase-linking jobs (no counterpart in the reference,
+ * which runs one module invocation per process).  fpl_server_submit queues a
+ * job whose buffers are host memory (valid, and preferably page-locked, until
+ * the job is done); a scheduler thread admits jobs in arrival order while
+ * their device footprint fits memory_budget, stages them on a copy stream,
+ * and runs waves of at most wave_pixels pixels in which every resident job
+ * gets a slice of rows -- jobs arriving during a wave join the next one
+ * (continuous batching).  Results are copied back as each job finishes.  A
+ * job's result does not depend on the other jobs in flight. */
+typedef struct fpl_server fpl_server;
+typedef struct {
+    size_t memory_budget;      /* device bytes for resident jobs (default 80 GB) */
+    long long wave_pixels;     /* pixels per wave (default 524288)              */
+    int device;
+} fpl_server_config;
+typedef struct {
+    double queue_ms;           /* submit -> admitted      */
+    double run_ms;             /* admitted -> results back */
+    double total_ms;           /* submit -> results back   */
+    int rc;
+} fpl_ticket_info;
+void fpl_server_config_default(fpl_server_config *cfg);
+int fpl_server_create(const fpl_server_config *cfg, fpl_server **out);
+int fpl_server_submit(fpl_server *srv, const fpl_job *job, unsigned long long *ticket);
+/* waits up to timeout_s for the job; 0 when its outputs are in place */
+int fpl_server_wait(fpl_server *srv, unsigned long long ticket, double timeout_s, fpl_ticket_info *info);
+int fpl_server_destroy(fpl_server *srv);
 
 /* ---- run without device allocation (no counterpart in the reference) -----
  * For callers that cannot call cudaMalloc -- an application whose device
