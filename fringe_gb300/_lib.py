@@ -83,6 +83,7 @@ _SIGS = {
                                        ctypes.POINTER(FplTicketInfo)]),
     "fpl_server_destroy": (ctypes.c_int, [_P]),
     "fpl_ctx_set_tuning": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
+    "fpl_adjust_wrapped": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_longlong, _P]),
     "fpl_ctx_last_error": (ctypes.c_char_p, [_P]),
     "fpl_ctx_set_profiling": (ctypes.c_int, [_P, ctypes.c_int]),
     "fpl_ctx_profile": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double),

@@ -52,6 +52,23 @@ int grow(fpl_ctx *ctx, void **p, size_t *cap, size_t need)
     return FPL_OK;
 }
 
+// wrapped datum adjustment (python/adjustMiniStacks.py:174-197: the "mul"
+// pixel function of a derived VRT band): out[d][p] = phase[d][p] * datum[p]
+__global__ void k_adjust_wrapped(const float2 *phase, const float2 *__restrict__ datum, float2 *out,
+                                 int ndates, long long npix)
+{
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
+         p += (long long)gridDim.x * blockDim.x) {
+        const float2 b = __ldg(datum + p);
+        for (int d = 0; d < ndates; ++d) {
+            const float2 a = phase[d * npix + p];
+            const double re = (double)a.x * b.x - (double)a.y * b.y;
+            const double im = (double)a.x * b.y + (double)a.y * b.x;
+            out[d * npix + p] = make_float2((float)re, (float)im);
+        }
+    }
+}
+
 }  // namespace
 
 int fpl_validate_job(const fpl_job *job)
@@ -226,15 +243,15 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
         ev = &ctx->prof_ev[3 * ctx->prof_used++];
         FPL_CUDA(ctx, cudaEventRecord(ev[0], st));
     }
-    const bool mixed = job->precision == FPL_PREC_MIXED && P.nb <= 32 && P.K <= 1024;
+    const bool mixed = job->precision == FPL_PREC_MIXED && fpl::gram_box_supported(P.nb, P.ny, P.nx);
     if (mixed) {
-        // tensor-core coherence matrices, then eigen-solves, chunk by chunk
-        // of rows so the packed matrices stay within a bounded buffer
-        const int npk = P.nb * (P.nb + 1) / 2;
+        // tensor-core Gamma records, then eigen-solves, chunk by chunk of
+        // rows so the records stay within a bounded buffer
+        const int rec = fpl::gram_box_record(P.nb);
         const long long chunk_px_max = std::max<long long>(P.cols, (1ll << 20));
         const int rows_per_chunk = (int)std::max<long long>(1, chunk_px_max / P.cols);
         const long long chunk_px = (long long)std::min(rows_per_chunk, r1 - r0) * P.cols;
-        if ((rc = grow(ctx, &ctx->d_cbuf, &ctx->cap_cbuf, sizeof(float2) * (size_t)npk * chunk_px))) return rc;
+        if ((rc = grow(ctx, &ctx->d_cbuf, &ctx->cap_cbuf, sizeof(float) * (size_t)rec * chunk_px))) return rc;
         if ((rc = grow(ctx, &ctx->d_cinfo, &ctx->cap_cinfo, sizeof(int) * (size_t)chunk_px))) return rc;
         for (int ra = r0; ra < r1; ra += rows_per_chunk) {
             const int rb = std::min(r1, ra + rows_per_chunk);
@@ -244,8 +261,8 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
             Q.cbuf = static_cast<float2 *>(ctx->d_cbuf);
             Q.cinfo = static_cast<int *>(ctx->d_cinfo);
             Q.cbase = Q.pix_begin;
-            Q.cstride = npk;
-            FPL_CUDA(ctx, fpl::launch_gram_tc(Q, ctx->num_sms, st));
+            Q.cstride = rec;
+            FPL_CUDA(ctx, fpl::launch_gram_box(Q, ctx->num_sms, st));
             FPL_CUDA(ctx, fpl::launch_solve(Q, ctx->num_sms, st));
         }
     } else {
@@ -258,6 +275,21 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
 }
 
 extern "C" {
+
+int fpl_adjust_wrapped(fpl_ctx *ctx, const void *phase, const void *datum, void *out,
+                       int ndates, long long npix, void *stream)
+{
+    if (!ctx || !phase || !datum || !out) return FPL_ERR_NULL;
+    if (ndates < 0 || npix < 0) return FPL_ERR_OPTIONS;
+    if (ndates == 0 || npix == 0) return FPL_OK;
+    FPL_CUDA(ctx, cudaSetDevice(ctx->device));
+    long long blocks = std::min<long long>((npix + 255) / 256, (long long)ctx->num_sms * 8);
+    k_adjust_wrapped<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float2 *>(phase), static_cast<const float2 *>(datum),
+        static_cast<float2 *>(out), ndates, npix);
+    FPL_CUDA(ctx, cudaGetLastError());
+    return FPL_OK;
+}
 
 int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream)
 {

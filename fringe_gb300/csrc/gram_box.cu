@@ -1,0 +1,519 @@
+// gram_box.cu -- coherence matrices on the 5th-generation tensor cores, one
+// tile of 128 pixels per GEMM.
+//
+// Mixed-precision form of the SHP gather + Gamma accumulation
+// (src/evd/evd.cpp:516-564, src/phase_link/phase_link.cpp:482-522).  For a
+// pixel p the reference sums x_q x_q^H over its SHPs q.  Written for a tile
+// of pixels at once this is a masked box filter of the per-sample outer
+// products,
+//     Gamma_p = sum_q m_pq x_q x_q^H,   m_pq = 1 iff q is an SHP of p,
+// which is a dense GEMM over the samples q of the union of the tile's windows:
+//     D[p][c] = sum_q A[p][q] B[c][q]
+//   A = the 0/1 SHP mask (exact in bf16), rows = the 128 pixels of an
+//       8 x 16 pixel tile, columns = the (8+Wy-1) x (16+Wx-1) union samples;
+//   B = the outer-product entries Re / Im x_qi conj(x_qj), formed in FP32
+//       (the reference's complex<float> products) and split into bf16
+//       hi + lo parts (16 significant bits), so D = A B_hi + A B_lo is
+//       accumulated in FP32 in tensor memory.
+// Each outer product is formed once per tile instead of once for every pixel
+// that uses it.  One thread issues tcgen05.mma (M = 128 pixels, N <= 256
+// Gamma entries, K = 16 samples); the Gamma entries are processed in passes
+// of 256 columns.
+//
+// Column order (the Gamma record read by the eigen kernel): dates padded to an
+// even count and grouped in pairs; block (a, b), a <= b, row-major over the
+// upper triangle of pairs, holds 8 floats: Re, Im of Gamma_ij for
+// (i, j) = (2a,2b), (2a,2b+1), (2a+1,2b), (2a+1,2b+1).
+//
+// Operand layout (no swizzle, K-major): core matrices of 8 rows x 16 bytes;
+// K-adjacent core matrices 128 B apart, 8-row groups KC*16+16 B apart (the
+// 16-byte pad keeps the staging stores free of bank conflicts).
+//
+// Samples whose value is non-finite, or whose components lie outside
+// [2^-50, 2^50] in magnitude (other than 0), are outside the range of the
+// split: they are zeroed in the tile and every pixel that has one among its
+// SHPs is handed to the FP64 path (CI_DEFER), which follows the reference
+// exactly.  Every wait on the tensor core is bounded; on timeout the CTA
+// records an error flag, stops, and frees its tensor memory after a second
+// bounded wait.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+#include "pixel.cuh"
+
+namespace fpl {
+namespace {
+
+constexpr int BX_THREADS = 256;
+constexpr int BX_TR = 8, BX_TC = 16, BX_M = 128;   // pixel tile (MMA M)
+constexpr int BX_NCOL = 256;                       // Gamma columns per pass (MMA N)
+constexpr int BX_MAXK = 2048;                      // union samples per tile
+constexpr int BX_MAXW = BX_MAXK / 32;              // union mask words per pixel
+constexpr int BX_MAXWX = 63;                       // window width (64-bit row extraction)
+constexpr int BX_MISC = 4096;
+constexpr int CI_SKIP = -100;                      // pixel outside this launch's rows
+constexpr unsigned ERR_TC_TIMEOUT = 2u;
+constexpr long long BX_SPIN_LIMIT = 1ll << 26;     // ~ seconds of polling
+
+template <int KC> struct BoxLay {
+    static constexpr int SBO = KC * 16 + 16;                 // bytes between 8-row groups
+    static constexpr int A_BYTES = (BX_M / 8) * SBO;
+    static constexpr int B_BYTES = (BX_NCOL / 8) * SBO;      // one of hi / lo
+    static constexpr int STAGE = A_BYTES + 2 * B_BYTES;
+    static constexpr int MAXPAIR = (KC == 64) ? 16 : 32;     // date pairs: 32 or 64 dates
+    static constexpr int XRS = KC * 16 + 16;                 // bytes per date-pair row of X
+    static constexpr int X_BYTES = MAXPAIR * XRS;
+    static constexpr size_t OFF_X = 2 * (size_t)STAGE;
+    static constexpr size_t OFF_MISC = OFF_X + X_BYTES;
+    static constexpr size_t OFF_U = OFF_MISC + BX_MISC;
+    static constexpr size_t MAX_SMEM = OFF_U + (size_t)BX_M * BX_MAXW * 4;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t make_smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor, kind::f16: FP32 accumulate, bf16 A and B, both
+// K-major, M = 128, N = n
+__device__ __forceinline__ uint32_t make_idesc(int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+        :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(smem_addr(mbar)) : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(mbar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// 32 consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *r)
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// len (<= 63) bits of a little-endian word array starting at bit pos
+__device__ __forceinline__ uint64_t extract_bits(const uint32_t *w, int nul, int pos, int len)
+{
+    const int w0 = pos >> 5, sh = pos & 31;
+    uint64_t v = w[w0];
+    if (w0 + 1 < nul) v |= (uint64_t)w[w0 + 1] << 32;
+    v >>= sh;
+    if (sh && w0 + 2 < nul) v |= (uint64_t)w[w0 + 2] << (64 - sh);
+    return v & ((1ull << len) - 1ull);
+}
+
+// 0 or a normal magnitude in [2^-50, 2^50]: the bf16 split of every product
+// of two such components stays normal and the window sums stay finite
+__device__ __forceinline__ bool split_range(float v)
+{
+    const float a = fabsf(v);
+    return v == 0.f || (a >= 8.8817842e-16f && a <= 1.1258999e15f);
+}
+
+// 8 values of one Gamma column into bf16 hi and lo rows (16 bytes each)
+__device__ __forceinline__ void store_split(unsigned char *dh, unsigned char *dl, const float *v)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const __nv_bfloat162 hb = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+        const uint32_t hu = *reinterpret_cast<const uint32_t *>(&hb);
+        const float h0 = __uint_as_float(hu << 16), h1 = __uint_as_float(hu & 0xffff0000u);
+        const __nv_bfloat162 lb = __floats2bfloat162_rn(v[2 * q] - h0, v[2 * q + 1] - h1);
+        h[q] = hu;
+        l[q] = *reinterpret_cast<const uint32_t *>(&lb);
+    }
+    *reinterpret_cast<uint4 *>(dh) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(dl) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+template <int KC>
+__global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
+{
+    using L = BoxLay<KC>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *Xb = smem + L::OFF_X;
+    unsigned char *misc = smem + L::OFF_MISC;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);                 // 2 stages
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(misc + 16);
+    uint32_t *badw = reinterpret_cast<uint32_t *>(misc + 32);            // [2][KC / 32]
+    int *pinfo = reinterpret_cast<int *>(misc + 64);                     // 128
+    int *pdefer = reinterpret_cast<int *>(misc + 64 + 512);              // 128
+    short2 *blk = reinterpret_cast<short2 *>(misc + 64 + 1024);          // <= 528 blocks
+    uint32_t *umask = reinterpret_cast<uint32_t *>(smem + L::OFF_U);     // [128][W]
+    uint32_t *nm = reinterpret_cast<uint32_t *>(smem + L::STAGE);        // nmap words (stage 1, mask build only)
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n = P.nb, dp = (n + 1) >> 1, nblk = dp * (dp + 1) / 2, ncolt = 8 * nblk;
+    const int cols = P.cols, rows = P.rows, nul = P.nulong;
+    const int wy = 2 * P.ny + 1, wx = P.wx;
+    const int uh = BX_TR + wy - 1, uw = BX_TC + wx - 1, uwp = (uw + 7) & ~7;
+    const int kp = (uh * uwp + KC - 1) / KC * KC, nchunk = kp / KC;
+    const int W = kp >> 5;
+    const int ra = int(P.pix_begin / cols), rb = ra + int(P.npix / cols);
+    const int ntc = (cols + BX_TC - 1) / BX_TC, ntr = (rb - ra + BX_TR - 1) / BX_TR;
+    const long long ntiles = (long long)ntc * ntr;
+    const int npass = (ncolt + BX_NCOL - 1) / BX_NCOL;
+    const int min_neigh = (P.semantics == SEM_PL) ? P.min_neigh : 2;   // evd.cpp:566
+    const long long plane = P.plane;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_addr(tmem_slot)), "r"(BX_NCOL) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int b = tid; b < nblk; b += BX_THREADS) {
+        int a = 0, rem = b;
+        while (rem >= dp - a) { rem -= dp - a; ++a; }
+        blk[b] = make_short2((short)a, (short)(a + rem));
+    }
+    if (tid < 2 * (KC / 32)) badw[tid] = 0;
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tbase = *tmem_slot;
+
+    uint32_t pend = 0, par = 0;     // per stage: MMAs in flight, barrier parity
+    unsigned gstep = 0;
+    bool timed_out = false;
+    // wait until the MMAs reading stage s are complete; the vote keeps the
+    // timeout decision uniform across the CTA
+    auto wait_stage = [&](int s) -> bool {
+        bool late = false;
+        if (pend & (1u << s)) {
+            long long spins = 0;
+            while (!mbar_try_wait(&mbar[s], (par >> s) & 1u)) {
+                if (++spins > BX_SPIN_LIMIT) { late = true; break; }
+            }
+            if (!late) { par ^= 1u << s; pend &= ~(1u << s); }
+        }
+        return __syncthreads_or(late) == 0;
+    };
+
+    for (long long t = blockIdx.x; t < ntiles && !timed_out; t += gridDim.x) {
+        const int R0 = ra + int(t / ntc) * BX_TR, C0 = int(t % ntc) * BX_TC;
+        // ---- per-pixel SHP masks over the union samples ----------------
+        for (int e = tid; e < BX_M * W; e += BX_THREADS) umask[e] = 0;
+        for (int e = tid; e < BX_M * nul; e += BX_THREADS) {
+            const int m = e / nul, w = e - m * nul;
+            const int r = R0 + m / BX_TC, c = C0 + m % BX_TC;
+            nm[e] = (r < rb && c < cols) ? __ldg(P.nmap + ((long long)r * cols + c) * nul + w) : 0u;
+        }
+        __syncthreads();
+        for (int e = tid; e < BX_M * wy; e += BX_THREADS) {
+            const int m = e / wy, a = e - m * wy;
+            const int tr = m / BX_TC, tc = m % BX_TC;
+            const int r = R0 + tr, c = C0 + tc;
+            const int sr = r - P.ny + a;                    // image row of window row a
+            if (r >= rb || c >= cols || sr < 0 || sr >= rows) continue;
+            uint64_t bits = extract_bits(nm + m * nul, nul, a * wx, wx);
+            // window column b is image column c - nx + b (evd.cpp:530-534)
+            const int blo = max(0, P.nx - c), bhi = min(wx, cols - c + P.nx);
+            if (bhi <= blo) continue;
+            bits &= ((1ull << (bhi - blo)) - 1ull) << blo;
+            if (!bits) continue;
+            const int pos = (tr + a) * uwp + tc;            // union sample of window (a, 0)
+            const int w0 = pos >> 5, sh = pos & 31;
+            const uint64_t lo = bits << sh;
+            const uint32_t hi = sh ? (uint32_t)(bits >> (64 - sh)) : 0u;
+            uint32_t *um = umask + m * W;
+            if ((uint32_t)lo) atomicOr(um + w0, (uint32_t)lo);
+            if ((uint32_t)(lo >> 32)) atomicOr(um + w0 + 1, (uint32_t)(lo >> 32));
+            if (hi) atomicOr(um + w0 + 2, hi);
+        }
+        __syncthreads();
+        if (tid < BX_M) {
+            const int m = tid, r = R0 + m / BX_TC, c = C0 + m % BX_TC;
+            int info = CI_SKIP;
+            if (r < rb && c < cols) {
+                const int cflat = P.ny * wx + P.nx;
+                if (!((nm[m * nul + (cflat >> 5)] >> (cflat & 31)) & 1u)) {
+                    info = CI_CENTRE;                       // evd.cpp:517
+                } else {
+                    int cnt = 0;
+                    for (int w = 0; w < W; ++w) cnt += __popc(umask[m * W + w]);
+                    info = (cnt < min_neigh) ? CI_FEW : cnt;
+                }
+            }
+            pinfo[m] = info;
+            pdefer[m] = 0;
+        }
+        // (the first chunk's barriers order these before any use)
+
+        for (int pass = 0; pass < npass && !timed_out; ++pass) {
+            const int cb = pass * BX_NCOL;
+            const int ncol = min(BX_NCOL, ncolt - cb);
+            const int nmma = (ncol + 15) & ~15;
+            const uint32_t idesc = make_idesc(nmma);
+            for (int ch = 0; ch < nchunk; ++ch) {
+                const int s = gstep & 1;
+                if (!wait_stage(s)) { timed_out = true; break; }
+                unsigned char *As = smem + s * L::STAGE;
+                unsigned char *Bh = As + L::A_BYTES, *Bl = Bh + L::B_BYTES;
+                uint32_t *bw = badw + s * (KC / 32);
+                const int k0 = ch * KC;
+                // ---- samples of the chunk, date pairs interleaved ----
+                {
+                    const int sidx = tid % KC;
+                    const int k = k0 + sidx;
+                    const int ur = k / uwp, uc = k - ur * uwp;
+                    const int r = R0 - P.ny + ur, c = C0 - P.nx + uc;
+                    const bool valid = uc < uw && ur < uh && r >= 0 && r < rows && c >= 0 && c < cols;
+                    const float2 *src = P.stack + (valid ? (long long)r * cols + c : 0ll);
+                    bool bad = false;
+                    for (int d = tid / KC; d < 2 * dp; d += BX_THREADS / KC) {
+                        float2 x = make_float2(0.f, 0.f);
+                        if (valid && d < n) {
+                            x = __ldg(src + d * plane);
+                            if (!split_range(x.x) || !split_range(x.y)) {
+                                bad = true;
+                                x = make_float2(0.f, 0.f);
+                            }
+                        }
+                        *reinterpret_cast<float2 *>(Xb + (d >> 1) * L::XRS + sidx * 16 + (d & 1) * 8) = x;
+                    }
+                    if (bad) atomicOr(bw + (sidx >> 5), 1u << (sidx & 31));
+                }
+                if (tid < KC / 32) badw[(s ^ 1) * (KC / 32) + tid] = 0;   // for the next chunk
+                __syncthreads();
+                // ---- A: SHP mask rows ----
+                for (int e = tid; e < BX_M * (KC / 8); e += BX_THREADS) {
+                    const int m = e & (BX_M - 1), k8 = e >> 7;
+                    const int b0 = k0 + k8 * 8;
+                    const uint32_t bits = (umask[m * W + (b0 >> 5)] >> (b0 & 31)) & 0xffu;
+                    const uint32_t bad = (bw[(k8 * 8) >> 5] >> ((k8 * 8) & 31)) & 0xffu;
+                    if (bits & bad) pdefer[m] = 1;
+                    uint32_t v[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        v[q] = ((bits >> (2 * q)) & 1u ? 0x3F80u : 0u) | ((bits >> (2 * q + 1)) & 1u ? 0x3F800000u : 0u);
+                    *reinterpret_cast<uint4 *>(As + (m >> 3) * L::SBO + k8 * 128 + (m & 7) * 16) =
+                        make_uint4(v[0], v[1], v[2], v[3]);
+                }
+                // ---- B: outer-product entries, hi and lo ----
+                for (int e = tid; e < 32 * (KC / 8); e += BX_THREADS) {
+                    const int bl = e & 31, k8 = e >> 5;
+                    if (bl * 8 >= nmma) continue;
+                    unsigned char *dh = Bh + bl * L::SBO + k8 * 128;
+                    unsigned char *dl = Bl + bl * L::SBO + k8 * 128;
+                    if (bl * 8 >= ncol) {
+                        const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            *reinterpret_cast<uint4 *>(dh + c * 16) = z;
+                            *reinterpret_cast<uint4 *>(dl + c * 16) = z;
+                        }
+                        continue;
+                    }
+                    const short2 ab = blk[cb / 8 + bl];
+                    const unsigned char *xa = Xb + ab.x * L::XRS + k8 * 128;
+                    const unsigned char *xb = Xb + ab.y * L::XRS + k8 * 128;
+                    float4 pa[8], pb[8];   // per sample: x_{2a}, x_{2a+1} / x_{2b}, x_{2b+1}
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) pa[q] = *reinterpret_cast<const float4 *>(xa + q * 16);
+                    if (ab.x != ab.y) {
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) pb[q] = *reinterpret_cast<const float4 *>(xb + q * 16);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) pb[q] = pa[q];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int ia = u >> 1, jb = u & 1;     // i = 2a + ia, j = 2b + jb
+                        float re[8], im[8];
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            const float xr = ia ? pa[q].z : pa[q].x, xi = ia ? pa[q].w : pa[q].y;
+                            const float yr = jb ? pb[q].z : pb[q].x, yi = jb ? pb[q].w : pb[q].y;
+                            re[q] = fmaf(xr, yr, xi * yi);          // Re x_i conj(x_j)
+                            im[q] = fmaf(xi, yr, -(xr * yi));       // Im x_i conj(x_j)
+                        }
+                        store_split(dh + (2 * u) * 16, dl + (2 * u) * 16, re);
+                        store_split(dh + (2 * u + 1) * 16, dl + (2 * u + 1) * 16, im);
+                    }
+                }
+                fence_async_smem();
+                __syncthreads();
+                if (tid == 0) {
+                    fence_after_sync();
+                    const uint32_t a0 = smem_addr(As), h0 = smem_addr(Bh), l0 = smem_addr(Bl);
+#pragma unroll
+                    for (int kk = 0; kk < KC / 16; ++kk) {
+                        const uint64_t da = make_smem_desc(a0 + kk * 256, 128, L::SBO);
+                        const uint64_t dh = make_smem_desc(h0 + kk * 256, 128, L::SBO);
+                        const uint64_t dl = make_smem_desc(l0 + kk * 256, 128, L::SBO);
+                        tc_mma(tbase, da, dh, idesc, (ch > 0 || kk > 0) ? 1u : 0u);
+                        tc_mma(tbase, da, dl, idesc, 1u);
+                    }
+                    tc_commit(&mbar[s]);
+                }
+                pend |= 1u << s;
+                ++gstep;
+            }
+            if (timed_out) break;
+            if (!wait_stage(0) || !wait_stage(1)) { timed_out = true; break; }
+            fence_after_sync();
+            // ---- epilogue: warp w reads TMEM lanes 32(w%4).., 128 columns ----
+            {
+                const int q = warp & 3, h = warp >> 2;
+                const int m = 32 * q + lane;
+                const bool store = pinfo[m] >= 0 && !pdefer[m];
+                const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
+                float *dst = reinterpret_cast<float *>(P.cbuf) + (store ? loc * P.cstride + cb : 0ll);
+                for (int c32 = 4 * h; c32 < 4 * h + 4; ++c32) {
+                    const int col0 = 32 * c32;
+                    if (col0 >= ncol) break;
+                    uint32_t v[32];
+                    tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)col0, v);
+                    tmem_wait_ld();
+                    if (store) {
+                        const int lim = min(32, ncol - col0);
+#pragma unroll
+                        for (int j = 0; j < 32; j += 4)
+                            if (j < lim)
+                                *reinterpret_cast<float4 *>(dst + col0 + j) =
+                                    make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
+                                                __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
+                    }
+                }
+            }
+            fence_before_sync();
+            __syncthreads();
+        }
+        if (timed_out) break;
+        if (tid < BX_M) {
+            const int m = tid, info = pinfo[m];
+            if (info != CI_SKIP) {
+                const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
+                P.cinfo[loc] = (info >= 0 && pdefer[m]) ? CI_DEFER : info;
+            }
+        }
+        __syncthreads();
+    }
+    if (timed_out) {
+        if (tid == 0) atomicOr(P.err, ERR_TC_TIMEOUT);
+        // give the MMAs in flight a second bounded wait before their tensor
+        // memory is released
+        for (int s = 0; s < 2; ++s) {
+            if (pend & (1u << s)) {
+                long long spins = 0;
+                while (!mbar_try_wait(&mbar[s], (par >> s) & 1u) && ++spins < BX_SPIN_LIMIT) {
+                }
+            }
+        }
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(BX_NCOL) : "memory");
+    }
+}
+
+template <int KC>
+cudaError_t launch_box_t(const KParams &P, int num_sms, cudaStream_t st)
+{
+    using L = BoxLay<KC>;
+    static bool configured[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && !configured[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(k_gram_box<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)L::MAX_SMEM);
+        if (e != cudaSuccess) return e;
+        configured[dev] = true;
+    }
+    const int uh = BX_TR + 2 * P.ny, uwp = (BX_TC + P.wx - 1 + 7) & ~7;
+    const int kp = (uh * uwp + KC - 1) / KC * KC;
+    const size_t smem = L::OFF_U + (size_t)BX_M * (kp / 32) * 4;
+    const long long nrows = P.npix / P.cols;
+    const long long ntiles = ((P.cols + BX_TC - 1) / BX_TC) * ((nrows + BX_TR - 1) / BX_TR);
+    long long blocks = num_sms;
+    if (ntiles < blocks) blocks = ntiles > 0 ? ntiles : 1;
+    k_gram_box<KC><<<(unsigned)blocks, BX_THREADS, smem, st>>>(P);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool gram_box_supported(int nb, int ny, int nx)
+{
+    const int wx = 2 * nx + 1;
+    if (nb < 1 || nb > 64 || wx > BX_MAXWX) return false;
+    const int uh = BX_TR + 2 * ny, uwp = (BX_TC + wx - 1 + 7) & ~7;
+    return (long long)uh * uwp <= BX_MAXK;
+}
+
+int gram_box_record(int nb)
+{
+    const int dp = (nb + 1) >> 1;
+    return 8 * (dp * (dp + 1) / 2);
+}
+
+cudaError_t launch_gram_box(const KParams &P, int num_sms, cudaStream_t st)
+{
+    if (!gram_box_supported(P.nb, P.ny, P.nx) || P.cols <= 0 || P.pix_begin % P.cols || P.npix % P.cols)
+        return cudaErrorInvalidValue;
+    if (P.npix == 0) return cudaSuccess;
+    return (P.nb <= 32) ? launch_box_t<64>(P, num_sms, st) : launch_box_t<32>(P, num_sms, st);
+}
+
+}  // namespace fpl

@@ -17,9 +17,17 @@ cudaError_t launch_fp32(const KParams &P, int num_sms, cudaStream_t st);
 // FP64 form over the work list in P (or over every pixel if P.fb_list is null)
 cudaError_t launch_fp64(const KParams &P, int num_sms, cudaStream_t st);
 
-// mixed form: tensor-core coherence matrices for P.npix pixels from
-// P.pix_begin into P.cbuf / P.cinfo (nbands <= 32)
-cudaError_t launch_gram_tc(const KParams &P, int num_sms, cudaStream_t st);
+// mixed form: is the tensor-core Gamma kernel available for this stack
+// depth and window (nbands <= 64, window width <= 63, window union of an
+// 8 x 16 pixel tile <= 2048 samples)
+bool gram_box_supported(int nb, int ny, int nx);
+
+// floats per Gamma record written by launch_gram_box
+int gram_box_record(int nb);
+
+// mixed form: tensor-core Gamma records for the whole rows
+// [P.pix_begin, P.pix_begin + P.npix) into P.cbuf / P.cinfo
+cudaError_t launch_gram_box(const KParams &P, int num_sms, cudaStream_t st);
 
 // mixed form: eigen-solves and outputs from P.cbuf / P.cinfo
 cudaError_t launch_solve(const KParams &P, int num_sms, cudaStream_t st);

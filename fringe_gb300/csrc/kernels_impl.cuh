@@ -32,7 +32,7 @@ __global__ void k_pixels(KParams P)
     }
 }
 
-// mixed form, second half: eigen-solves from tensor-core coherence matrices
+// mixed form, second half: eigen-solves from the tensor-core Gamma records
 template <int NP>
 __global__ void k_solve(KParams P)
 {
@@ -44,7 +44,7 @@ __global__ void k_solve(KParams P)
     const long long nw = (long long)gridDim.x * warps;
     for (long long q = gw; q < P.npix; q += nw) {
         const long long pp = P.pix_begin + q;
-        const int npix = pixel_load_coherence<NP>(P, pp, sm, lane);
+        const int npix = pixel_load_gamma<NP>(P, pp, sm, lane);
         if (npix >= 0) pixel_solve<float, NP>(P, pp, sm, lane, npix);
     }
 }

@@ -49,14 +49,14 @@ struct KParams {
     int fb_cap;
     unsigned *err;                      // error flags (scratch)
     int *slow;                          // pixels that left the fast eigen path (scratch)
-    // mixed form: packed coherence matrices from the tensor-core kernel
-    float2 *cbuf;                       // [pixel - cbase][n(n+1)/2], rows of the upper triangle
+    // mixed form: Gamma records from the tensor-core kernel
+    float2 *cbuf;                       // [pixel - cbase][cstride floats] (pixel_load_gamma)
     int *cinfo;                         // [pixel - cbase]: SHP count, or CI_* below
     long long cbase;                    // first pixel of the buffers
-    int cstride;                        // n(n+1)/2
+    int cstride;                        // floats per record
 };
 
-enum { CI_CENTRE = -1, CI_FEW = -2, CI_BAD = -3 };
+enum { CI_CENTRE = -1, CI_FEW = -2, CI_DEFER = -3 };
 
 enum { M_MLE = 0, M_EVD = 1, M_STBAS = 2 };
 enum { SEM_EVD = 0, SEM_PL = 1 };
@@ -818,6 +818,61 @@ __device__ __forceinline__ void put_code(const KParams &P, long long pp, int lan
 // Gather, Gamma and coherence (evd.cpp:514-582).  Returns the SHP count
 // with C in the warp's slab, or -1 when the pixel is finished (skipped or
 // coded) and its outputs are written.
+// Gamma (upper triangle and diagonal of the warp's C slab) to coherence
+// (evd.cpp:569-582, phase_link.cpp:527-538): C_ij = Gamma_ij / sqrt(P_i P_j),
+// lower triangle by conjugation, unit diagonal.  A non-finite result is
+// reported as the failure of the first eigen call; returns false then.
+template <typename T, int NP>
+__device__ bool gamma_to_coherence(const KParams &P, long long pp, unsigned char *sm, int lane)
+{
+    using L = Lay<T, NP>;
+    constexpr int LD = L::LD;
+    C2<T> *Cm = reinterpret_cast<C2<T> *>(sm + L::cm);
+    T *yv = reinterpret_cast<T *>(sm + L::yy);
+    const int n = P.nb;
+    const bool plink = (P.semantics == SEM_PL);
+    bool bad = false;
+    for (int i = lane; i < n; i += 32) {
+        T Pi = Cm[i * LD + i].x;
+        bad |= !(Pi > T(0)) || !isfinite(Pi);
+        yv[i] = T(1) / sqrt(Pi);
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    __syncwarp();
+    if (!bad) {
+        for (int i = lane; i < n; i += 32) {
+            const T ri = yv[i];
+            for (int j = i + 1; j < n; ++j) {
+                C2<T> g = Cm[i * LD + j];
+                C2<T> c;
+                if (sizeof(T) == 8) {
+                    T den = sqrt(Cm[i * LD + i].x * Cm[j * LD + j].x);
+                    c = cmk<T>(g.x / den, g.y / den);
+                } else {
+                    c = cscale(g, ri * yv[j]);
+                }
+                bad |= !isfinite(c.x) || !isfinite(c.y);
+                Cm[i * LD + j] = c;
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) {
+            for (int j = 0; j < i; ++j) Cm[i * LD + j] = cconj(Cm[j * LD + i]);
+        }
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) Cm[i * LD + i] = cmk<T>(T(1), T(0));
+        bad = __any_sync(0xffffffffu, bad);
+        __syncwarp();
+    }
+    if (bad) {
+        // non-finite coherence: LAPACK's answer on NaN input is undefined;
+        // the first eigen call is reported as failed.
+        put_code(P, pp, lane, (!plink && P.method != M_MLE) ? -6 : -1);
+        return false;
+    }
+    return true;
+}
+
 template <typename T, int NP>
 __device__ int pixel_coherence(const KParams &P, long long pp, unsigned char *sm, int lane)
 {
@@ -967,48 +1022,7 @@ __device__ int pixel_coherence(const KParams &P, long long pp, unsigned char *sm
         return -1;
     }
 
-    // ---- coherence (evd.cpp:569-582) -------------------------------------
-    {
-        bool bad = false;
-        for (int i = lane; i < n; i += 32) {
-            T Pi = Cm[i * LD + i].x;
-            bad |= !(Pi > T(0)) || !isfinite(Pi);
-            yv[i] = T(1) / sqrt(Pi);
-        }
-        bad = __any_sync(0xffffffffu, bad);
-        __syncwarp();
-        if (!bad) {
-            for (int i = lane; i < n; i += 32) {
-                const T ri = yv[i];
-                for (int j = i + 1; j < n; ++j) {
-                    C2<T> g = Cm[i * LD + j];
-                    C2<T> c;
-                    if (sizeof(T) == 8) {
-                        T den = sqrt(Cm[i * LD + i].x * Cm[j * LD + j].x);
-                        c = cmk<T>(g.x / den, g.y / den);
-                    } else {
-                        c = cscale(g, ri * yv[j]);
-                    }
-                    bad |= !isfinite(c.x) || !isfinite(c.y);
-                    Cm[i * LD + j] = c;
-                }
-            }
-            __syncwarp();
-            for (int i = lane; i < n; i += 32) {
-                for (int j = 0; j < i; ++j) Cm[i * LD + j] = cconj(Cm[j * LD + i]);
-            }
-            __syncwarp();
-            for (int i = lane; i < n; i += 32) Cm[i * LD + i] = cmk<T>(T(1), T(0));
-            bad = __any_sync(0xffffffffu, bad);
-            __syncwarp();
-        }
-        if (bad) {
-            // non-finite coherence: LAPACK's answer on NaN input is undefined;
-            // the first eigen call is reported as failed.
-            put_code(P, pp, lane, (!plink && P.method != M_MLE) ? -6 : -1);
-            return -1;
-        }
-    }
+    if (!gamma_to_coherence<T, NP>(P, pp, sm, lane)) return -1;
     return npix;
 }
 
@@ -1318,11 +1332,15 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
 }
 
 
-// Mixed form: the coherence C of pixel pp was formed on the tensor cores
-// (gram_tc.cu) and stored as the packed upper triangle; load it into the
-// warp's slab.  Returns the SHP count, or -1 when the pixel is finished.
+// Mixed form: Gamma of pixel pp was accumulated on the tensor cores
+// (gram_box.cu) into a record of P.cstride floats; load it into the warp's
+// slab and normalise it to coherence.  Record layout: dates padded to an even
+// count and grouped in pairs; block (a, b), a <= b < DP, row-major over the
+// upper triangle of pairs, holds Re, Im of Gamma_ij for (i, j) = (2a,2b),
+// (2a,2b+1), (2a+1,2b), (2a+1,2b+1).  Returns the SHP count, or -1 when the
+// pixel is finished (or handed to the FP64 path).
 template <int NP>
-__device__ int pixel_load_coherence(const KParams &P, long long pp, unsigned char *sm, int lane)
+__device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *sm, int lane)
 {
     using L = Lay<float, NP>;
     constexpr int LD = L::LD;
@@ -1340,23 +1358,27 @@ __device__ int pixel_load_coherence(const KParams &P, long long pp, unsigned cha
         if (P.status && lane == 0) P.status[pp] = (info == CI_CENTRE) ? 1 : 2;
         return -1;
     }
-    if (info == CI_BAD) {
-        const bool plink = (P.semantics == SEM_PL);
-        put_code(P, pp, lane, (!plink && P.method != M_MLE) ? -6 : -1);
+    if (info == CI_DEFER) {
+        defer_fp64(P, pp, lane);
         return -1;
     }
-    const float2 *src = P.cbuf + loc * P.cstride;
-    int off = 0;
-    for (int i = 0; i < n; ++i) {
-        for (int j = i + lane; j < n; j += 32) {
-            const float2 v = src[off + (j - i)];
-            Cm[i * LD + j] = cmk<float>(v.x, v.y);
-            Cm[j * LD + i] = cmk<float>(v.x, -v.y);
+    const float *rec = reinterpret_cast<const float *>(P.cbuf) + loc * (long long)P.cstride;
+    const int dp = (n + 1) >> 1;
+    int base = 0;                                   // first block of pair row a
+    for (int a = 0; a < dp; ++a) {
+        for (int b = a + lane; b < dp; b += 32) {
+            const float4 *blk = reinterpret_cast<const float4 *>(rec + 8 * (base + b - a));
+            const float4 u = blk[0], v = blk[1];
+            const int i0 = 2 * a, i1 = 2 * a + 1, j0 = 2 * b, j1 = 2 * b + 1;
+            if (j0 < n) Cm[i0 * LD + j0] = cmk<float>(u.x, u.y);
+            if (j1 < n) Cm[i0 * LD + j1] = cmk<float>(u.z, u.w);
+            if (i1 < n && j0 >= i1) Cm[i1 * LD + j0] = cmk<float>(v.x, v.y);
+            if (j1 < n) Cm[i1 * LD + j1] = cmk<float>(v.z, v.w);
         }
-        off += n - i;
+        base += dp - a;
     }
     __syncwarp();
-    return info;
+    return gamma_to_coherence<float, NP>(P, pp, sm, lane) ? info : -1;
 }
 
 template <typename T, int NP>

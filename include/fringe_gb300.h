@@ -257,6 +257,15 @@ void fpl_options_default(fpl_options *opts);
 /* File-level run; returns 0 or the reference's module codes. */
 int fpl_process(const fpl_options *opts);
 
+/* Wrapped-phase datum adjustment of the sequential estimator: for the
+ * ndates dates of one ministack, out[d][p] = phase[d][p] * datum[p]
+ * (complex64, product in double).  Replaces the derived VRT band with pixel
+ * function "mul" that python/adjustMiniStacks.py:174-197 writes per date
+ * (called from adjust_wrapped, :203-223).  Device pointers; enqueued on
+ * `stream` (NULL = the legacy default stream); out may alias phase. */
+int fpl_adjust_wrapped(fpl_ctx *ctx, const void *phase, const void *datum, void *out,
+                       int ndates, long long npix, void *stream);
+
 /* Human-readable text for a return code. */
 const char *fpl_error_string(int code);
 

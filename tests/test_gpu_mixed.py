@@ -36,3 +36,77 @@ def test_mixed_large_window_chunks(gpu_lib):
     g = phase_link(stack, nmap, (8, 10), method="MLE", precision="mixed")
     o = oracle.run(stack, nmap, 8, 10, method="MLE")
     assert_parity(compare(g, o), phase_tol=1e-3, tcorr_tol=2e-4)
+
+
+def _mixed_and_oracle(stack, nmap, ny, nx, **kw):
+    from fringe_gb300 import phase_link
+    g = phase_link(stack, nmap, (ny, nx), precision="mixed", want_status=True, **kw)
+    okw = {k: v for k, v in kw.items() if k in ("method", "semantics", "min_neighbors", "rows")}
+    o = oracle.run(stack, nmap, ny, nx, **okw)
+    return g, o
+
+
+@pytest.mark.parametrize("nb", [1, 2, 5, 16, 17, 33, 64])
+def test_mixed_depths(gpu_lib, nb):
+    """Every stack depth: odd counts pad the date pairs, more than 32 dates
+    take the 32-sample chunk layout."""
+    stack, nmap = synth.scene("voronoi", 20, 24, nb, 2, 3, seed=100 + nb)
+    for method, sem in (("MLE", "evd"), ("EVD", "evd"), ("MLE", "phase_link")):
+        g, o = _mixed_and_oracle(stack, nmap, 2, 3, method=method, semantics=sem)
+        assert_parity(compare(g, o), phase_tol=1e-3, tcorr_tol=2e-4)
+        if nb == 1:
+            assert np.array_equal(np.isnan(g["tcorr"]), np.isnan(o["tcorr"]))
+
+
+def test_mixed_illconditioned_n64(gpu_lib):
+    stack, nmap = synth.scene("illcond", 24, 40, 64, 5, 10, seed=1003)
+    for method, sem in (("MLE", "evd"), ("MLE", "phase_link"), ("EVD", "evd")):
+        g, o = _mixed_and_oracle(stack, nmap, 5, 10, method=method, semantics=sem)
+        assert_parity(compare(g, o), phase_tol=1e-3, tcorr_tol=2e-4)
+
+
+def test_mixed_edge_masks_and_shapes(gpu_lib):
+    stack, nmap = synth.scene("uniform", 12, 15, 8, 2, 2, seed=5)
+    g, o = _mixed_and_oracle(stack, np.zeros_like(nmap), 2, 2, method="MLE")
+    assert not np.any(g["phase"]) and not np.any(g["tcorr"]) and np.all(g["status"] == 1)
+    c = np.zeros_like(nmap)
+    flat = 2 * 5 + 2
+    c[..., flat // 32] = np.uint32(1 << (flat % 32))
+    g, o = _mixed_and_oracle(stack, c, 2, 2, method="EVD")
+    assert not np.any(g["phase"]) and np.all(g["status"] == 2)
+    # scenes smaller than one 8 x 16 tile, single rows / columns, partial tiles
+    for shape in ((3, 4), (1, 17), (19, 1), (1, 1), (9, 17), (17, 33)):
+        st, nm = synth.scene("uniform", shape[0], shape[1], 6, 5, 10, seed=9)
+        for method in ("MLE", "EVD"):
+            g, o = _mixed_and_oracle(st, nm, 5, 10, method=method)
+            assert_parity(compare(g, o), phase_tol=1e-3, tcorr_tol=2e-4)
+    g, o = _mixed_and_oracle(stack, nmap, 2, 2, method="MLE", semantics="phase_link", min_neighbors=26)
+    assert not np.any(g["tcorr"]) and not np.any(o["tcorr"])
+
+
+def test_mixed_row_range(gpu_lib):
+    from fringe_gb300 import phase_link
+    stack, nmap = synth.scene("voronoi", 40, 36, 12, 3, 5, seed=21)
+    full = phase_link(stack, nmap, (3, 5), method="MLE", precision="mixed")
+    part = phase_link(stack, nmap, (3, 5), method="MLE", precision="mixed", rows=(5, 30))
+    # tiles start at the first row of the range: same sums, other grouping
+    m = compare({k: v[..., 5:30, :] for k, v in part.items()},
+                {k: v[..., 5:30, :] for k, v in full.items()})
+    assert_parity(m, phase_tol=1e-4, tcorr_tol=1e-5)
+    assert not np.any(part["tcorr"][:5]) and not np.any(part["tcorr"][30:])
+
+
+def test_mixed_out_of_range_samples(gpu_lib):
+    """NaN samples, and magnitudes outside the bf16 split's range, send the
+    pixels whose SHPs include them to the FP64 path; other pixels of the same
+    tile are unaffected."""
+    stack, nmap = synth.scene("uniform", 24, 40, 10, 2, 3, seed=77)
+    stack[2, 5, 7] = np.nan
+    stack[:, 15, 30] = 3e17
+    stack[4, 20, 3] = 1e-17 + 1e-17j
+    for method, sem in (("MLE", "evd"), ("EVD", "evd"), ("MLE", "phase_link")):
+        g, o = _mixed_and_oracle(stack, nmap, 2, 3, method=method, semantics=sem)
+        m = compare(g, o)
+        assert_parity(m, phase_tol=1e-3, tcorr_tol=2e-4)
+        # the NaN neighbourhood reports the oracle's codes
+        assert np.array_equal(g["tcorr"][3:8, 4:11] < 0, o["tcorr"][3:8, 4:11] < 0)
