@@ -24,9 +24,9 @@ cudaError_t launch_fp32(const KParams &P, int num_sms, cudaStream_t st)
 cudaError_t launch_solve(const KParams &P, int num_sms, cudaStream_t st)
 {
     switch (pick_np(P.nb)) {
-    case 16: return launch_solve_t<16>(P, num_sms, st);
-    case 32: return launch_solve_t<32>(P, num_sms, st);
-    case 64: return launch_solve_t<64>(P, num_sms, st);
+    case 16: return launch_solve_t<16, true>(P, num_sms, st);
+    case 32: return launch_solve_t<32, true>(P, num_sms, st);
+    case 64: return launch_solve_t<64, false>(P, num_sms, st);
     }
     return cudaErrorInvalidValue;
 }

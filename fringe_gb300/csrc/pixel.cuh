@@ -129,8 +129,7 @@ template <typename T, int NP> struct Lay {
     static constexpr int LD = NP + 1;        // matrix row stride (odd: conflict-free columns)
     static constexpr int XS = NP + 2;        // staging row stride in float2 (16-byte rows)
     static constexpr size_t mat = sizeof(C2<T>) * NP * LD;
-    static constexpr size_t cm = 0;                                   // coherence C
-    static constexpr size_t wm = align16(cm + mat);                   // work: staging / Cholesky / M / tridiag
+    static constexpr size_t wm = 0;                                   // work: staging / Cholesky / M / tridiag
     static constexpr size_t wm_bytes = align16(cmax(mat, sizeof(float2) * 32 * XS));
     static constexpr size_t xr = wm + align16(mat / 2);               // real sweep matrix: upper half of wm
     static constexpr size_t vv = wm + wm_bytes;                       // complex vector v
@@ -142,8 +141,130 @@ template <typename T, int NP> struct Lay {
     static constexpr size_t yy = align16(e2 + sizeof(T) * NP);        // y / row k / 1/sqrt(P)
     static constexpr size_t wk = align16(yy + sizeof(T) * NP);        // 5*NP scratch (lane 0)
     static constexpr size_t ph = align16(wk + sizeof(T) * 5 * NP);    // phases (float2)
-    static constexpr size_t bytes = align16(ph + sizeof(float2) * NP);
+    // the coherence C comes last: kernels that keep C in tensor memory
+    // allocate only bytes_noc per warp
+    static constexpr size_t bytes_noc = align16(ph + sizeof(float2) * NP);
+    static constexpr size_t cm = bytes_noc;                           // coherence C
+    static constexpr size_t bytes = cm + align16(mat);
 };
+
+// ------------------------------------------------------------------------
+// Access to the rows of the coherence C.  Lane l owns rows l and l + 32;
+// rows are read and written in chunks of 8 complex entries (columns 8c ..
+// 8c+7).  Every lane of the warp calls load / store together (the tensor-
+// memory form requires it); rows >= NP read as zero.
+// ------------------------------------------------------------------------
+template <typename T, int NP> struct CRowsSmem {
+    C2<T> *C;
+    int lane;
+    __device__ __forceinline__ void load(int h, int c, C2<T> (&v)[8]) const
+    {
+        const int i = lane + 32 * h;
+        const C2<T> *r = C + i * (NP + 1) + 8 * c;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = (i < NP) ? r[k] : cmk<T>(T(0), T(0));
+    }
+    __device__ __forceinline__ void store(int h, int c, const C2<T> (&v)[8]) const
+    {
+        const int i = lane + 32 * h;
+        if (i >= NP) return;
+        C2<T> *r = C + i * (NP + 1) + 8 * c;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) r[k] = v[k];
+    }
+    __device__ __forceinline__ void fence() const { __syncwarp(); }
+};
+
+// C in tensor memory (FP32, NP <= 32): the warp owns 2*NP 32-bit columns
+// of its 32 TMEM lanes; lane l holds row l (Re, Im interleaved).  The solver
+// kernels issue no MMA: tensor memory is extra per-warp storage there,
+// which frees shared memory for more resident warps.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
+        :: "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+           "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+        : "memory");
+}
+
+template <int NP> struct CRowsTmem {
+    static_assert(NP <= 32, "one row per lane");
+    uint32_t taddr;      // lane quadrant << 16 | first column of the warp
+    __device__ __forceinline__ void load(int h, int c, C2<float> (&v)[8]) const
+    {
+        uint32_t r[16];
+        tmem_ld16(taddr + 16u * (uint32_t)c, r);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = cmk<float>(__uint_as_float(r[2 * k]), __uint_as_float(r[2 * k + 1]));
+    }
+    __device__ __forceinline__ void store(int h, int c, const C2<float> (&v)[8]) const
+    {
+        uint32_t r[16];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            r[2 * k] = __float_as_uint(v[k].x);
+            r[2 * k + 1] = __float_as_uint(v[k].y);
+        }
+        tmem_st16(taddr + 16u * (uint32_t)c, r);
+    }
+    __device__ __forceinline__ void fence() const
+    {
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+};
+
+// number of row slots (h) and 8-entry chunks (c) per lane
+template <int NP> struct RowShape {
+    static constexpr int H = (NP + 31) / 32;
+    static constexpr int CH = NP / 8;
+};
+
+// y = C x through a row policy (lane-distributed x in smem xv, y in y0 / y1)
+template <typename T, int NP, typename CP>
+__device__ void rows_matvec(const CP &cp, int n, const C2<T> *xv, C2<T> &y0, C2<T> &y1, int lane)
+{
+#pragma unroll
+    for (int h = 0; h < RowShape<NP>::H; ++h) {
+        C2<T> a = cmk<T>(T(0), T(0));
+#pragma unroll 1
+        for (int c = 0; c < RowShape<NP>::CH; ++c) {
+            C2<T> v[8];
+            cp.load(h, c, v);
+#pragma unroll
+            for (int k = 0; k < 8; k += 2) {
+                const int j = 8 * c + k;
+                C2<T> x0, x1;
+                if (sizeof(T) == 4) {
+                    const float4 q = *reinterpret_cast<const float4 *>(xv + j);
+                    x0 = cmk<T>(T(q.x), T(q.y));
+                    x1 = cmk<T>(T(q.z), T(q.w));
+                } else {
+                    x0 = xv[j];
+                    x1 = xv[j + 1];
+                }
+                if (j < n) cfma(a, v[k], x0);
+                if (j + 1 < n) cfma(a, v[k + 1], x1);
+            }
+        }
+        const int i = lane + 32 * h;
+        if (i >= n) a = cmk<T>(T(0), T(0));
+        if (h == 0) y0 = a; else y1 = a;
+    }
+    if (RowShape<NP>::H == 1) y1 = cmk<T>(T(0), T(0));
+}
 
 // ------------------------------------------------------------------------
 // warp Cholesky (lower, in place) of the complex Hermitian matrix in A:
@@ -235,14 +356,26 @@ __device__ void warp_chol_solve(const C2<T> *L, int n, C2<T> &b0, C2<T> &b1, int
 
 // lambda_min(A) vs thr for a complex Hermitian A (lower triangle read):
 // +1 certainly above, -1 certainly at or below, 0 inside [thr-delta, thr+delta].
-template <typename T, int LD, int NP>
-__device__ int lam_min_test_c(const C2<T> *A, C2<T> *W, C2<T> *col, int n, T thr, T delta, int lane)
+template <typename T, int LD, int NP, typename CP>
+__device__ int lam_min_test_c(const CP &cp, C2<T> *W, C2<T> *col, int n, T thr, T delta, int lane)
 {
     const int nsh = delta > T(0) ? 2 : 1;
     for (int s = 0; s < nsh; ++s) {
         T sh = (nsh == 1) ? thr : (s == 0 ? thr + delta : thr - delta);
         __syncwarp();
-        for (int e = lane; e < n * LD; e += 32) W[e] = A[e];
+#pragma unroll
+        for (int h = 0; h < RowShape<NP>::H; ++h) {
+            const int i = lane + 32 * h;
+#pragma unroll 1
+            for (int c = 0; c < RowShape<NP>::CH; ++c) {
+                C2<T> v[8];
+                cp.load(h, c, v);
+                if (i < NP) {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) W[i * LD + 8 * c + k] = v[k];
+                }
+            }
+        }
         __syncwarp();
         for (int i = lane; i < n; i += 32) W[i * LD + i].x -= sh;
         __syncwarp();
@@ -596,12 +729,11 @@ __device__ T warp_eigpair(C2<T> *W, int n, int index, T lo_hint, T hi_hint, unsi
 // Largest eigenvector of the Hermitian C by power iteration.  Returns true
 // with z (lane-distributed) when the residual test passes; false when the
 // iteration converges too slowly (the caller then uses the Householder path).
-template <typename T, int NP>
-__device__ bool warp_power(const C2<T> *C, int n, unsigned char *sm, int lane, C2<T> &z0, C2<T> &z1,
+template <typename T, int NP, typename CP>
+__device__ bool warp_power(const CP &cp, int n, unsigned char *sm, int lane, C2<T> &z0, C2<T> &z1,
                            T *lam_out)
 {
     using L = Lay<T, NP>;
-    constexpr int LD = L::LD;
     C2<T> *vv = reinterpret_cast<C2<T> *>(sm + L::vv);
     const int i0 = lane, i1 = lane + 32;
     // start: row sums (C * 1)
@@ -611,28 +743,7 @@ __device__ bool warp_power(const C2<T> *C, int n, unsigned char *sm, int lane, C
     const T tol = (sizeof(T) == 4) ? T(4e-6) : T(1e-13);
     for (int it = 0; it < 96; ++it) {
         C2<T> u[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int i = lane + 32 * h;
-            u[h] = cmk<T>(T(0), T(0));
-            if (h * 32 >= NP || i >= n) continue;
-            const C2<T> *Ci = C + i * LD;
-            C2<T> a0 = cmk<T>(T(0), T(0)), a1 = cmk<T>(T(0), T(0));
-            for (int j = 0; j < n; j += 2) {
-                C2<T> v0, v1;
-                if (sizeof(T) == 4) {
-                    float4 q = *reinterpret_cast<const float4 *>(vv + j);
-                    v0 = cmk<T>(T(q.x), T(q.y));
-                    v1 = cmk<T>(T(q.z), T(q.w));
-                } else {
-                    v0 = vv[j];
-                    v1 = vv[j + 1];
-                }
-                cfma(a0, Ci[j], v0);
-                if (j + 1 < n) cfma(a1, Ci[j + 1], v1);
-            }
-            u[h] = cadd(a0, a1);
-        }
+        rows_matvec<T, NP>(cp, n, vv, u[0], u[1], lane);
         // rho = v^H u (v normalised after the first pass), residual u - rho v
         const C2<T> v0 = (i0 < n) ? vv[i0] : cmk<T>(T(0), T(0));
         const C2<T> v1 = (NP > 32 && i1 < n) ? vv[i1] : cmk<T>(T(0), T(0));
@@ -695,8 +806,8 @@ __device__ void warp_matvec(const C2<T> *A, int n, const C2<T> *xv, C2<T> &y0, C
 // A few power iterations on C from the all-ones vector: a start vector for
 // the MLE inverse iteration (the EVD and MLE solutions are close).  Leaves
 // the normalised vector lane-distributed in z0 / z1 and in vv.
-template <typename T, int NP>
-__device__ void warp_power_start(const C2<T> *C, int n, int iters, unsigned char *sm, int lane,
+template <typename T, int NP, typename CP>
+__device__ void warp_power_start(const CP &cp, int n, int iters, unsigned char *sm, int lane,
                                  C2<T> &z0, C2<T> &z1)
 {
     using L = Lay<T, NP>;
@@ -705,7 +816,7 @@ __device__ void warp_power_start(const C2<T> *C, int n, int iters, unsigned char
     __syncwarp();
     for (int it = 0; it < iters; ++it) {
         C2<T> u0, u1;
-        warp_matvec<T, L::LD, NP>(C, n, vv, u0, u1, lane);
+        rows_matvec<T, NP>(cp, n, vv, u0, u1, lane);
         const T inv = rsqrt_t(warp_sum(cabs2(u0) + cabs2(u1)));
         z0 = cscale(u0, inv);
         z1 = cscale(u1, inv);
@@ -823,11 +934,10 @@ __device__ __forceinline__ void put_code(const KParams &P, long long pp, int lan
 // lower triangle by conjugation, unit diagonal.  A non-finite result is
 // reported as the failure of the first eigen call; returns false then.
 template <typename T, int NP>
-__device__ bool gamma_to_coherence(const KParams &P, long long pp, unsigned char *sm, int lane)
+__device__ bool gamma_to_coherence(const KParams &P, long long pp, C2<T> *Cm, unsigned char *sm, int lane)
 {
     using L = Lay<T, NP>;
     constexpr int LD = L::LD;
-    C2<T> *Cm = reinterpret_cast<C2<T> *>(sm + L::cm);
     T *yv = reinterpret_cast<T *>(sm + L::yy);
     const int n = P.nb;
     const bool plink = (P.semantics == SEM_PL);
@@ -1022,19 +1132,21 @@ __device__ int pixel_coherence(const KParams &P, long long pp, unsigned char *sm
         return -1;
     }
 
-    if (!gamma_to_coherence<T, NP>(P, pp, sm, lane)) return -1;
+    if (!gamma_to_coherence<T, NP>(P, pp, Cm, sm, lane)) return -1;
     return npix;
 }
 
 
-// Eigen-solve and outputs for a pixel whose coherence C is in the warp's
-// slab (evd.cpp:584-786, phase_link.cpp:540-665).
-template <typename T, int NP>
-__device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, int lane, int npix)
+// Eigen-solve and outputs for a pixel whose coherence C is reached through
+// the row policy cp (the warp's slab, or tensor memory), evd.cpp:584-786,
+// phase_link.cpp:540-665.
+template <typename T, int NP, typename CP>
+__device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, int lane, int npix,
+                            const CP &cp)
 {
     using L = Lay<T, NP>;
+    using RS = RowShape<NP>;
     constexpr int LD = L::LD;
-    C2<T> *Cm = reinterpret_cast<C2<T> *>(sm + L::cm);
     C2<T> *Wm = reinterpret_cast<C2<T> *>(sm + L::wm);
     T *Xr = reinterpret_cast<T *>(sm + L::xr);
     T *yv = reinterpret_cast<T *>(sm + L::yy);
@@ -1056,18 +1168,45 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             for (int j = 0; j < nn; ++j) s += cabs2(A[i * LD + j]);
         return sqrt(warp_sum(s));
     };
+    auto fro_c = [&]() {
+        T s = T(0);
+#pragma unroll
+        for (int h = 0; h < RS::H; ++h) {
+            const int i = lane + 32 * h;
+#pragma unroll 1
+            for (int c = 0; c < RS::CH; ++c) {
+                C2<T> v[8];
+                cp.load(h, c, v);
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (i < nn && 8 * c + k < nn) s += cabs2(v[k]);
+            }
+        }
+        return sqrt(warp_sum(s));
+    };
     // |C| into Xr (unit diagonal), then its sweep inverse.  Returns
     // +1 inverted (X = inv|C| in Xr), -1 not positive definite, 0 undecided
     // in FP32 (rounding band or condition too large).
     auto abs_inverse = [&]() -> int {
         T rs = T(0);
-        for (int i = lane; i < nn; i += 32) {
+#pragma unroll
+        for (int h = 0; h < RS::H; ++h) {
+            const int i = lane + 32 * h;
             T s = T(0);
-            for (int j = 0; j < nn; ++j) {
-                const T m2 = cabs2(Cm[i * LD + j]);
-                T a = (i == j) ? T(1) : (fp32 ? m2 * rsqrt_t(max(m2, T(1e-37))) : sqrt(m2));
-                Xr[i * LD + j] = a;
-                s += a;
+#pragma unroll 1
+            for (int c = 0; c < RS::CH; ++c) {
+                C2<T> v[8];
+                cp.load(h, c, v);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int j = 8 * c + k;
+                    const T m2 = cabs2(v[k]);
+                    const T a = (i == j) ? T(1) : (fp32 ? m2 * rsqrt_t(max(m2, T(1e-37))) : sqrt(m2));
+                    if (i < nn && j < nn) {
+                        Xr[i * LD + j] = a;
+                        s += a;
+                    }
+                }
             }
             rs = max(rs, s);
         }
@@ -1091,8 +1230,8 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
                 put_code(P, pp, lane, -2);
                 return;
             }
-            const T dC = fp32 ? amb * fro(Cm) : T(0);
-            int r = lam_min_test_c<T, LD, NP>(Cm, Wm, col, n, thr, dC, lane);
+            const T dC = fp32 ? amb * fro_c() : T(0);
+            int r = lam_min_test_c<T, LD, NP>(cp, Wm, col, n, thr, dC, lane);
             if (r == 0) { defer_fp64(P, pp, lane); return; }
             if (r < 0) { put_code(P, pp, lane, -2); return; }
             // |C| check (evd.cpp:623-644) and inverse (evd.cpp:652-664).
@@ -1119,9 +1258,20 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
                     // decide with the Cholesky test of |C| - 1e-6 I (this work
                     // matrix overlaps the inverse, which is then recomputed)
                     __syncwarp();
-                    for (int i = lane; i < n; i += 32) {
-                        for (int j = 0; j <= i; ++j)
-                            Wm[i * LD + j] = cmk<T>((i == j) ? T(1) - thr : sqrt(cabs2(Cm[i * LD + j])), T(0));
+#pragma unroll
+                    for (int h = 0; h < RS::H; ++h) {
+                        const int i = lane + 32 * h;
+#pragma unroll 1
+                        for (int c = 0; c < RS::CH; ++c) {
+                            C2<T> v[8];
+                            cp.load(h, c, v);
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {
+                                const int j = 8 * c + k;
+                                if (i < n && j <= i)
+                                    Wm[i * LD + j] = cmk<T>((i == j) ? T(1) - thr : sqrt(cabs2(v[k])), T(0));
+                            }
+                        }
                     }
                     __syncwarp();
                     if (!warp_chol_c<T, LD, NP>(Wm, n, col, lane)) {
@@ -1145,10 +1295,22 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             mode = 0;
         } else {
             if (P.method == M_STBAS) {                       // evd.cpp:695-706
-                for (int i = lane; i < n; i += 32)
-                    for (int j = 0; j < n; ++j)
-                        if (j - i > P.bw || i - j > P.bw) Cm[i * LD + j] = cmk<T>(T(0), T(0));
-                __syncwarp();
+#pragma unroll
+                for (int h = 0; h < RS::H; ++h) {
+                    const int i = lane + 32 * h;
+#pragma unroll 1
+                    for (int c = 0; c < RS::CH; ++c) {
+                        C2<T> v[8];
+                        cp.load(h, c, v);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const int j = 8 * c + k;
+                            if (j - i > P.bw || i - j > P.bw) v[k] = cmk<T>(T(0), T(0));
+                        }
+                        cp.store(h, c, v);
+                    }
+                }
+                cp.fence();
             }
             mode = 1;
         }
@@ -1170,16 +1332,22 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         // M = inv(|C|) o C (evd.cpp:667); Xr shares bytes with Wm, so each
         // lane reads its inverse row into registers before M is written.
         auto form_M = [&]() {
-            for (int base = 0; base < nn; base += 32) {
-                const int i = base + lane;
+#pragma unroll
+            for (int h = 0; h < RS::H; ++h) {
+                const int i = lane + 32 * h;
                 T xrow[NP];
 #pragma unroll
                 for (int j = 0; j < NP; ++j) xrow[j] = (i < nn && j < nn) ? Xr[i * LD + j] : T(0);
                 __syncwarp();
-                if (i < nn) {
 #pragma unroll
-                    for (int j = 0; j < NP; ++j)
-                        if (j < nn) Wm[i * LD + j] = cscale(Cm[i * LD + j], xrow[j]);
+                for (int c = 0; c < RS::CH; ++c) {
+                    C2<T> v[8];
+                    cp.load(h, c, v);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const int j = 8 * c + k;
+                        if (i < nn && j < nn) Wm[i * LD + j] = cscale(v[k], xrow[j]);
+                    }
                 }
                 __syncwarp();
             }
@@ -1197,7 +1365,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         if (fp32) {
             // inverse iteration from the EVD direction, shifted just below
             // the Rayleigh quotient (the smallest eigenvalue is close to 1)
-            warp_power_start<T, NP>(Cm, n, 4, sm, lane, z0, z1);
+            warp_power_start<T, NP>(cp, n, 4, sm, lane, z0, z1);
             C2<T> *vv = reinterpret_cast<C2<T> *>(sm + L::vv);
             C2<T> m0, m1;
             warp_matvec<T, LD, NP>(Wm, n, vv, m0, m1, lane);
@@ -1239,11 +1407,21 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         }
     } else {
         T lam;
-        bool ok = warp_power<T, NP>(Cm, n, sm, lane, z0, z1, &lam);
+        bool ok = warp_power<T, NP>(cp, n, sm, lane, z0, z1, &lam);
         if (!ok) {
             if (lane == 0 && fp32) atomicAdd(P.slow, 1);
-            for (int i = lane; i < n; i += 32)
-                for (int j = 0; j < n; ++j) Wm[i * LD + j] = Cm[i * LD + j];
+#pragma unroll
+            for (int h = 0; h < RS::H; ++h) {
+                const int i = lane + 32 * h;
+#pragma unroll 1
+                for (int c = 0; c < RS::CH; ++c) {
+                    C2<T> v[8];
+                    cp.load(h, c, v);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if (i < n && 8 * c + k < n) Wm[i * LD + 8 * c + k] = v[k];
+                }
+            }
             __syncwarp();
             lam = warp_eigpair<T, NP>(Wm, n, n, T(0.999), T(1e30), sm, lane, z0, z1);
         }
@@ -1305,20 +1483,30 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         const bool stbas = (P.method == M_STBAS);
         T sr = T(0), si = T(0);
         int cnt = 0;
-        for (int i = lane; i < n; i += 32) {
-            const int ulim = stbas ? min(i + P.bw + 1, n) : n;
-            const float2 pi = phs[i];
+#pragma unroll
+        for (int h = 0; h < RS::H; ++h) {
+            const int i = lane + 32 * h;
+            const int ulim = (i < n) ? (stbas ? min(i + P.bw + 1, n) : n) : 0;
+            const float2 pi = (i < n) ? phs[i] : make_float2(0.f, 0.f);
             const C2<T> cpi = cmk<T>(T(pi.x), T(pi.y));
-            for (int j = i + 1; j < ulim; ++j) {
-                const C2<T> c = Cm[i * LD + j];
-                const T ca2 = cabs2(c);
-                const C2<T> u = (ca2 > T(0)) ? cscale(c, rsqrt_t(ca2)) : cmk<T>(T(1), T(0));
-                const float2 pj = phs[j];
-                // exp(i(arg C_ij - arg ph_i + arg ph_j))
-                const C2<T> v = cmul(cmulc(u, cpi), cmk<T>(T(pj.x), T(pj.y)));
-                sr += v.x;
-                si += v.y;
-                cnt++;
+#pragma unroll 1
+            for (int cc = 0; cc < RS::CH; ++cc) {
+                C2<T> cv[8];
+                cp.load(h, cc, cv);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int j = 8 * cc + k;
+                    if (j <= i || j >= ulim) continue;
+                    const C2<T> c = cv[k];
+                    const T ca2 = cabs2(c);
+                    const C2<T> u = (ca2 > T(0)) ? cscale(c, rsqrt_t(ca2)) : cmk<T>(T(1), T(0));
+                    const float2 pj = phs[j];
+                    // exp(i(arg C_ij - arg ph_i + arg ph_j))
+                    const C2<T> v = cmul(cmulc(u, cpi), cmk<T>(T(pj.x), T(pj.y)));
+                    sr += v.x;
+                    si += v.y;
+                    cnt++;
+                }
             }
         }
         sr = warp_sum(sr);
@@ -1333,18 +1521,17 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
 
 
 // Mixed form: Gamma of pixel pp was accumulated on the tensor cores
-// (gram_box.cu) into a record of P.cstride floats; load it into the warp's
-// slab and normalise it to coherence.  Record layout: dates padded to an even
+// (gram_box.cu) into a record of P.cstride floats; load it into the shared-
+// memory matrix Cm of the warp and normalise it to coherence.  Record layout: dates padded to an even
 // count and grouped in pairs; block (a, b), a <= b < DP, row-major over the
 // upper triangle of pairs, holds Re, Im of Gamma_ij for (i, j) = (2a,2b),
 // (2a,2b+1), (2a+1,2b), (2a+1,2b+1).  Returns the SHP count, or -1 when the
 // pixel is finished (or handed to the FP64 path).
 template <int NP>
-__device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *sm, int lane)
+__device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *sm, int lane, C2<float> *Cm)
 {
     using L = Lay<float, NP>;
     constexpr int LD = L::LD;
-    C2<float> *Cm = reinterpret_cast<C2<float> *>(sm + L::cm);
     const int n = P.nb;
     const long long plane = P.plane;
     for (int b = lane; b < n; b += 32) P.phase[b * plane + pp] = make_float2(0.f, 0.f);
@@ -1378,14 +1565,35 @@ __device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *s
         base += dp - a;
     }
     __syncwarp();
-    return gamma_to_coherence<float, NP>(P, pp, sm, lane) ? info : -1;
+    return gamma_to_coherence<float, NP>(P, pp, Cm, sm, lane) ? info : -1;
+}
+
+// rows of the shared-memory matrix A into the row policy cp
+template <typename T, int NP, typename CP>
+__device__ void rows_from_smem(const CP &cp, const C2<T> *A, int lane)
+{
+#pragma unroll
+    for (int h = 0; h < RowShape<NP>::H; ++h) {
+        const int i = lane + 32 * h;
+#pragma unroll 1
+        for (int c = 0; c < RowShape<NP>::CH; ++c) {
+            C2<T> v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = (i < NP) ? A[i * (NP + 1) + 8 * c + k] : cmk<T>(T(0), T(0));
+            cp.store(h, c, v);
+        }
+    }
+    cp.fence();
 }
 
 template <typename T, int NP>
 __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm, int lane)
 {
     const int npix = pixel_coherence<T, NP>(P, pp, sm, lane);
-    if (npix >= 0) pixel_solve<T, NP>(P, pp, sm, lane, npix);
+    if (npix >= 0) {
+        const CRowsSmem<T, NP> cp{reinterpret_cast<C2<T> *>(sm + Lay<T, NP>::cm), lane};
+        pixel_solve<T, NP>(P, pp, sm, lane, npix, cp);
+    }
 }
 
 }  // namespace fpl
