@@ -8,12 +8,21 @@ classes on seeded Voronoi cells, nmap = same-class neighbours (SHP counts
 20..231), MLE with the reference evd semantics.  One step phase-links the
 whole scene.
 
+Forms: the headline form is the mixed-precision one (tensor-core BF16
+hi/lo Gamma + FP32 eigen-solves, FP64 only where an FP32 decision is
+ambiguous); the plain FP32 form is timed beside it in the same run
+(``other_form``, ``mixed_over_fp32``).
+
 value : px/s with the stack and nmap resident in HBM (device pointers, no
         copies in the timed region).  The 1 GB stack exceeds the 129 MB L2,
         so no L2 flush is needed between steps.
 e2e   : px/s through the C ABI with pinned HOST buffers: every step copies the
         stack + nmap to the device and phase + tcorr + compressed SLC back.
-roofline : the FP32 pixel kernel, timed with CUDA events on its stream.
+kernels / roofline : per-kernel CUDA-event times on the launching stream;
+        the roofline object describes the kernel with the largest share.
+accuracy_vs_fp64 : phase RMS and temporal-coherence error of each form
+        against the FP64 form of the same kernels over the whole scene, with
+        validity-code mismatches counted separately.
 cpu_baseline : the oracle port (CPU restatement of the reference loop) on the
         host cores, on a bounded row sample of the same scene.
 
@@ -48,7 +57,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--method", default="MLE", choices=["MLE", "EVD", "STBAS"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed"],
+                    help="headline form (the other form is timed beside it)")
+    ap.add_argument("--no-compare", action="store_true", help="skip the other form")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the error statistics against the FP64 form")
     ap.add_argument("--rows", type=int, default=ROWS)
     ap.add_argument("--cols", type=int, default=COLS)
     ap.add_argument("--cpu-rows", type=int, default=0,
@@ -246,6 +259,71 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def device_form(phase_link, d_stack, d_nmap, ctx, precision, method, steps, warmup, dist, local):
+    """Times `steps` device-resident runs of one form; returns its figures
+    and its outputs (kept on the device for the accuracy comparison)."""
+    import torch
+    nb, R, C = d_stack.shape
+    out = {"phase": torch.zeros((nb, R, C), dtype=torch.complex64, device="cuda"),
+           "tcorr": torch.zeros((R, C), dtype=torch.float32, device="cuda"),
+           "comp": torch.zeros((R, C), dtype=torch.complex64, device="cuda")}
+    kw = dict(method=method, precision=precision, ctx=ctx, out=out)
+    for _ in range(max(3, warmup)):
+        phase_link(d_stack, d_nmap, (NY, NX), **kw)
+    torch.cuda.synchronize()
+    ctx.set_profiling(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        phase_link(d_stack, d_nmap, (NY, NX), **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    _, _, runs = ctx.profile()
+    kms = {k: v / max(runs, 1) for k, v in ctx.profile_kernels().items()}
+    ctx.set_profiling(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    # kernels of one step: FP32 pixel kernel + FP64 settle, or per chunk of
+    # rows (<= 2^20 pixels) the Gamma and solve kernels, then the FP64 settle
+    if precision == "mixed":
+        rows_per_chunk = max(1, max(C, 1 << 20) // C)
+        launches = 2 * (-(-R // rows_per_chunk)) + 1
+    else:
+        launches = 2
+    return {"ms": ms, "kernel_ms": kms, "clocks": clk, "launches_per_step": launches}, out
+
+
+def accuracy(out, ref, valid_ref):
+    """Phase and coherence error of one form against the FP64 form, over the
+    pixels valid in both; validity-code mismatches counted separately."""
+    import torch
+    tc, tr = out["tcorr"], ref["tcorr"]
+    code_a = torch.where(tc < 0, tc, torch.zeros_like(tc))
+    code_b = torch.where(tr < 0, tr, torch.zeros_like(tr))
+    mism = int((code_a != code_b).sum().item())
+    both = (tc > 0) & valid_ref
+    d = torch.angle(out["phase"][:, both] * torch.conj(ref["phase"][:, both]))
+    rms = float(torch.sqrt(torch.mean(d.double() ** 2)).item()) if d.numel() else 0.0
+    per_px = torch.sqrt(torch.mean(d.double() ** 2, dim=0)) if d.numel() else torch.zeros(1)
+    dt = (tc[both] - tr[both]).abs()
+    return {"phase_rms_rad": rms, "phase_rms_p999_rad": float(torch.quantile(per_px.float()[:1 << 24], 0.999).item()),
+            "phase_max_abs_rad": float(d.abs().max().item()) if d.numel() else 0.0,
+            "tcorr_max_abs": float(dt.max().item()) if dt.numel() else 0.0,
+            "tcorr_rms": float(torch.sqrt(torch.mean(dt.double() ** 2)).item()) if dt.numel() else 0.0,
+            "code_mismatch_px": mism, "compared_px": int(both.sum().item())}
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -272,46 +350,42 @@ def main():
     shp = popcount_words(nmap)
     sbar = float(shp.mean())
 
-    # ---- device-resident run (value) --------------------------------------
+    # ---- device-resident runs (value): the headline form, then the other -----
     d_stack = torch.from_numpy(stack).cuda()
     d_nmap = torch.from_numpy(nmap.view(np.int32)).cuda()
-    out = {"phase": torch.zeros((NB, R, C), dtype=torch.complex64, device="cuda"),
-           "tcorr": torch.zeros((R, C), dtype=torch.float32, device="cuda"),
-           "comp": torch.zeros((R, C), dtype=torch.complex64, device="cuda")}
-    kw = dict(method=args.method, precision=args.precision, ctx=ctx, out=out)
-    for _ in range(max(3, args.warmup)):
-        phase_link(d_stack, d_nmap, (NY, NX), **kw)
-    torch.cuda.synchronize()
-    fp64_px = None
-    ctx.set_profiling(True)
-    ctx.profile()
-    clocks = ClockSampler(local)
-    clocks.start()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        phase_link(d_stack, d_nmap, (NY, NX), **kw)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    clk = clocks.stop()
-    k32_ms, k64_ms, runs = ctx.profile()
-    ctx.set_profiling(False)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+    other = "fp32" if args.precision == "mixed" else "mixed"
+    forms = [args.precision] + ([] if args.no_compare else [other])
+    res, outs = {}, {}
+    for prec in forms:
+        res[prec], outs[prec] = device_form(phase_link, d_stack, d_nmap, ctx, prec, args.method,
+                                            args.steps, args.warmup, dist, local)
+    head = res[args.precision]
+    ms = head["ms"]
     value = world * npx * args.steps / (ms / 1e3)
-    tc = out["tcorr"].cpu().numpy()
+    tc = outs[args.precision]["tcorr"].cpu().numpy()
     valid = int((tc > 0).sum())
+
+    # ---- accuracy of both forms against the FP64 form (whole scene) -----------
+    acc = None
+    if not args.no_accuracy:
+        ref = {"phase": torch.zeros_like(outs[args.precision]["phase"]),
+               "tcorr": torch.zeros_like(outs[args.precision]["tcorr"]),
+               "comp": torch.zeros_like(outs[args.precision]["comp"])}
+        ctx.set_tuning(force_fp64=True)
+        t0 = time.perf_counter()
+        phase_link(d_stack, d_nmap, (NY, NX), method=args.method, ctx=ctx, out=ref)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        ctx.set_tuning(force_fp64=False)
+        vref = ref["tcorr"] > 0
+        acc = {p: accuracy(outs[p], ref, vref) for p in forms}
+        acc["fp64_form_s"] = t64
+        acc["reference"] = "FP64 form of the same kernels (all pixels FP64, pinned to the oracle)"
+        del ref
 
     # ---- end to end through the C ABI with pinned host buffers ---------------
     e2e = None
+    fp64_px = None
     if not args.no_e2e:
         h_stack = torch.from_numpy(stack).pin_memory()
         h_nmap = torch.from_numpy(nmap.view(np.int32)).pin_memory()
@@ -345,19 +419,38 @@ def main():
     if rank != 0:
         return
     hbm_peak, tf_peak, peak_src = load_peaks()
-    # dominant kernel: the FP32 pixel kernel, average launch duration
-    k_ms = k32_ms / max(runs, 1)
     centre = shp > 0
     flops = float((4.0 * NB * (NB + 1) * shp[centre]).sum())     # Gamma, Hermitian half
-    achieved_tf = flops / (k_ms / 1e3) / 1e12
     alg_bytes = npx * (16 * NB + 4 * nmap.shape[2] + 12)
+    km = head["kernel_ms"]
+    if args.precision == "mixed":
+        # dominant kernel of the mixed form by device time
+        dom = "solve" if km["solve"] >= km["gram"] else "gram"
+    else:
+        dom = "fp32"
+    names = {"fp32": "k_pixels<float> (FP32 SIMT gather + Gamma + eigen-solves)",
+             "gram": "k_gram_box (tcgen05 bf16 hi/lo Gamma, TMEM accumulate)",
+             "solve": "k_solve (warp eigen-solves from the Gamma records)"}
+    k_ms = km[dom]
+    achieved_tf = flops / (k_ms / 1e3) / 1e12
     traffic = None
     tf_path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tf_path):
         with open(tf_path) as f:
             tj = json.load(f)
-        if tj.get("kernel_bytes_per_px"):
-            traffic = tj["kernel_bytes_per_px"] * npx
+        ent = tj.get(dom) if isinstance(tj.get(dom), dict) else None
+        if ent and ent.get("kernel_bytes_per_px"):
+            traffic = ent["kernel_bytes_per_px"] * npx
+    per_kernel = {}
+    for k, v in km.items():
+        if v <= 0:
+            continue
+        e = {"ms_per_step": v}
+        if k in ("fp32", "gram"):
+            e["gamma_tflops"] = flops / (v / 1e3) / 1e12
+            e["frac_of_bf16_peak"] = e["gamma_tflops"] / tf_peak
+        e["path_bytes_gbs"] = alg_bytes / (v / 1e3) / 1e9
+        per_kernel[k] = e
     line = {
         "metric": METRIC, "value": value, "unit": "px/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -370,16 +463,24 @@ def main():
                    "l2": "inputs (1.0 GB stack) exceed L2; no flush needed",
                    "valid_px": valid, "fp64_settled_px": fp64_px},
         "e2e": e2e,
-        "gpu_launches": 2 * args.steps,
-        "clocks": clk,
+        "gpu_launches": head["launches_per_step"] * args.steps,
+        "clocks": head["clocks"],
         "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": tf_peak,
                      "unit": "TFLOP/s", "frac": achieved_tf / tf_peak, "traffic": traffic,
-                     "peak_source": peak_src,
-                     "kernel": "k_pixels<float> (FP32 SIMT Gamma + eigen-solves)",
-                     "kernel_ms": k_ms, "fp64_kernel_ms": k64_ms / max(runs, 1),
+                     "peak_source": peak_src, "kernel": names[dom],
+                     "work": "Gamma flops 4N(N+1)S summed over pixels, per step",
+                     "kernel_ms": k_ms,
                      "hbm_achieved_gbs": alg_bytes / (k_ms / 1e3) / 1e9,
                      "hbm_peak_gbs": hbm_peak},
+        "kernels": per_kernel,
     }
+    if not args.no_compare:
+        o = res[other]
+        line["other_form"] = {"precision": other, "value": world * npx * args.steps / (o["ms"] / 1e3),
+                              "ms_per_step": o["ms"] / args.steps, "kernel_ms": o["kernel_ms"]}
+        line["mixed_over_fp32"] = (res["fp32"]["ms"] / res["mixed"]["ms"])
+    if acc is not None:
+        line["accuracy_vs_fp64"] = acc
     if not args.no_serve and world == 1:
         line["serving"] = serving_measurement(args.serve_jobs)
     if not args.no_cpu:

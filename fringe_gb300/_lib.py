@@ -89,6 +89,7 @@ _SIGS = {
     "fpl_ctx_profile": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_int)]),
+    "fpl_ctx_profile_kernels": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
 }
 _EXTRA = {}
 
@@ -174,6 +175,14 @@ class Context:
         check(load().fpl_ctx_profile(self.handle, ctypes.byref(a), ctypes.byref(b),
                                      ctypes.byref(n)), self.handle)
         return a.value, b.value, n.value
+
+    def profile_kernels(self):
+        """Per-kernel milliseconds of the runs read by the last profile():
+        {"fp32": plain pixel kernel, "gram": tensor-core Gamma, "solve":
+        eigen-solves of the mixed form, "fp64": FP64 settle pass}."""
+        ms = (ctypes.c_double * 4)()
+        check(load().fpl_ctx_profile_kernels(self.handle, ms, 4), self.handle)
+        return dict(zip(("fp32", "gram", "solve", "fp64"), list(ms)))
 
     def set_tuning(self, amb_scale=-1.0, force_fp64=False):
         check(load().fpl_ctx_set_tuning(self.handle, float(amb_scale), int(force_fp64)), self.handle)

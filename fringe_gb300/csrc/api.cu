@@ -233,16 +233,24 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
         FPL_CUDA(ctx, fpl::launch_fp64(Q, ctx->num_sms, st));
         return FPL_OK;
     }
-    cudaEvent_t *ev = nullptr;
-    if (ctx->profile) {
-        while (ctx->prof_ev.size() < 3 * (ctx->prof_used + 1)) {
+    // optional per-kernel event pairs (fpl_ctx_set_profiling)
+    auto timed = [&](int tag, auto &&launch) -> cudaError_t {
+        if (!ctx->profile) return launch();
+        const size_t p = ctx->prof_tag.size();
+        while (ctx->prof_ev.size() < 2 * (p + 1)) {
             cudaEvent_t e;
-            FPL_CUDA(ctx, cudaEventCreate(&e));
+            cudaError_t ce = cudaEventCreate(&e);
+            if (ce != cudaSuccess) return ce;
             ctx->prof_ev.push_back(e);
         }
-        ev = &ctx->prof_ev[3 * ctx->prof_used++];
-        FPL_CUDA(ctx, cudaEventRecord(ev[0], st));
-    }
+        cudaError_t ce = cudaEventRecord(ctx->prof_ev[2 * p], st);
+        if (ce != cudaSuccess) return ce;
+        if ((ce = launch()) != cudaSuccess) return ce;
+        if ((ce = cudaEventRecord(ctx->prof_ev[2 * p + 1], st)) != cudaSuccess) return ce;
+        ctx->prof_tag.push_back(tag);
+        return cudaSuccess;
+    };
+    if (ctx->profile) ctx->prof_runs++;
     const bool mixed = job->precision == FPL_PREC_MIXED && fpl::gram_box_supported(P.nb, P.ny, P.nx);
     if (mixed) {
         // tensor-core Gamma records, then eigen-solves, chunk by chunk of
@@ -262,15 +270,13 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
             Q.cinfo = static_cast<int *>(ctx->d_cinfo);
             Q.cbase = Q.pix_begin;
             Q.cstride = rec;
-            FPL_CUDA(ctx, fpl::launch_gram_box(Q, ctx->num_sms, st));
-            FPL_CUDA(ctx, fpl::launch_solve(Q, ctx->num_sms, st));
+            FPL_CUDA(ctx, timed(FPL_KTAG_GRAM, [&] { return fpl::launch_gram_box(Q, ctx->num_sms, st); }));
+            FPL_CUDA(ctx, timed(FPL_KTAG_SOLVE, [&] { return fpl::launch_solve(Q, ctx->num_sms, st); }));
         }
     } else {
-        FPL_CUDA(ctx, fpl::launch_fp32(P, ctx->num_sms, st));
+        FPL_CUDA(ctx, timed(FPL_KTAG_FP32, [&] { return fpl::launch_fp32(P, ctx->num_sms, st); }));
     }
-    if (ev) FPL_CUDA(ctx, cudaEventRecord(ev[1], st));
-    FPL_CUDA(ctx, fpl::launch_fp64(P, ctx->num_sms, st));
-    if (ev) FPL_CUDA(ctx, cudaEventRecord(ev[2], st));
+    FPL_CUDA(ctx, timed(FPL_KTAG_FP64, [&] { return fpl::launch_fp64(P, ctx->num_sms, st); }));
     return FPL_OK;
 }
 
@@ -392,27 +398,34 @@ int fpl_ctx_set_profiling(fpl_ctx *ctx, int on)
 {
     if (!ctx) return FPL_ERR_NULL;
     ctx->profile = on != 0;
-    ctx->prof_used = 0;
+    ctx->prof_tag.clear();
+    ctx->prof_runs = 0;
     return FPL_OK;
 }
 
 int fpl_ctx_profile(fpl_ctx *ctx, double *fp32_ms, double *fp64_ms, int *runs)
 {
     if (!ctx) return FPL_ERR_NULL;
-    double a = 0.0, b = 0.0;
-    for (size_t r = 0; r < ctx->prof_used; ++r) {
-        cudaEvent_t *ev = &ctx->prof_ev[3 * r];
-        FPL_CUDA(ctx, cudaEventSynchronize(ev[2]));
-        float x = 0.f, y = 0.f;
-        FPL_CUDA(ctx, cudaEventElapsedTime(&x, ev[0], ev[1]));
-        FPL_CUDA(ctx, cudaEventElapsedTime(&y, ev[1], ev[2]));
-        a += x;
-        b += y;
+    double ms[FPL_KTAG_COUNT] = {};
+    for (size_t p = 0; p < ctx->prof_tag.size(); ++p) {
+        FPL_CUDA(ctx, cudaEventSynchronize(ctx->prof_ev[2 * p + 1]));
+        float x = 0.f;
+        FPL_CUDA(ctx, cudaEventElapsedTime(&x, ctx->prof_ev[2 * p], ctx->prof_ev[2 * p + 1]));
+        ms[ctx->prof_tag[p]] += x;
     }
-    if (fp32_ms) *fp32_ms = a;
-    if (fp64_ms) *fp64_ms = b;
-    if (runs) *runs = (int)ctx->prof_used;
-    ctx->prof_used = 0;
+    for (int t = 0; t < FPL_KTAG_COUNT; ++t) ctx->prof_ms[t] = ms[t];
+    if (fp32_ms) *fp32_ms = ms[FPL_KTAG_FP32] + ms[FPL_KTAG_GRAM] + ms[FPL_KTAG_SOLVE];
+    if (fp64_ms) *fp64_ms = ms[FPL_KTAG_FP64];
+    if (runs) *runs = (int)ctx->prof_runs;
+    ctx->prof_tag.clear();
+    ctx->prof_runs = 0;
+    return FPL_OK;
+}
+
+int fpl_ctx_profile_kernels(const fpl_ctx *ctx, double *ms, int count)
+{
+    if (!ctx || !ms) return FPL_ERR_NULL;
+    for (int t = 0; t < count && t < FPL_KTAG_COUNT; ++t) ms[t] = ctx->prof_ms[t];
     return FPL_OK;
 }
 

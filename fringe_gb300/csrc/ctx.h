@@ -34,10 +34,13 @@ struct fpl_ctx {
     float amb_scale = kDefaultAmbScale;
     float cond_max = kDefaultCondMax;
     bool force_fp64 = false;
-    // optional per-kernel timing: one event triple per enqueued run
+    // optional per-kernel timing: an event pair around every compute launch,
+    // tagged with the kernel (enum fpl_kernel_tag)
     bool profile = false;
-    std::vector<cudaEvent_t> prof_ev;   // 3 per run: before FP32, between, after FP64
-    size_t prof_used = 0;
+    std::vector<cudaEvent_t> prof_ev;   // event pool; pair p = events 2p, 2p+1
+    std::vector<int> prof_tag;          // tag of pair p
+    size_t prof_runs = 0;               // runs enqueued since the last read
+    double prof_ms[FPL_KTAG_COUNT] = {};   // per-tag sums of the last read
     fpl_stats stats = {};
     // autotuned warps per CTA of batch launches, keyed by (depth, taps, SHP density)
     std::map<long long, int> tuned_warps;

@@ -224,6 +224,17 @@ int fpl_ctx_set_tuning(fpl_ctx *ctx, float amb_scale, int force_fp64);
  * kernel milliseconds and the run count, and resets the record. */
 int fpl_ctx_set_profiling(fpl_ctx *ctx, int on);
 int fpl_ctx_profile(fpl_ctx *ctx, double *fp32_ms, double *fp64_ms, int *runs);
+/* Per-kernel split of the runs read by the last fpl_ctx_profile call:
+ * ms[tag] for tag < FPL_KTAG_COUNT (the FP32 figure of fpl_ctx_profile is
+ * FPL_KTAG_FP32 + FPL_KTAG_GRAM + FPL_KTAG_SOLVE, the FP64 one FPL_KTAG_FP64). */
+enum fpl_kernel_tag {
+    FPL_KTAG_FP32 = 0,       /* plain FP32 pixel kernel (gather + Gamma + solve) */
+    FPL_KTAG_GRAM = 1,       /* mixed form: tensor-core Gamma records            */
+    FPL_KTAG_SOLVE = 2,      /* mixed form: eigen-solves from the records        */
+    FPL_KTAG_FP64 = 3,       /* FP64 settle pass                                 */
+    FPL_KTAG_COUNT = 4
+};
+int fpl_ctx_profile_kernels(const fpl_ctx *ctx, double *ms, int count);
 
 /* ---- file-level module call ------------------------------------------------
  * Mirrors evdOptions (src/evd/evd.hpp:19-54; src/phase_link/phase_link.hpp:20-57)
