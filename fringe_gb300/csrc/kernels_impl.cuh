@@ -44,7 +44,7 @@ __device__ __forceinline__ int tmem_cols_for(int warps, int np)
 }
 
 template <int NP, bool TM>
-__global__ void k_solve(KParams P)
+__global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve(KParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warps = blockDim.x >> 5;
@@ -69,11 +69,9 @@ __global__ void k_solve(KParams P)
         C2<float> *A = reinterpret_cast<C2<float> *>(sm + Lay<float, NP>::wm);
         for (long long q = gw; q < P.npix; q += nw) {
             const long long pp = P.pix_begin + q;
-            const int npix = pixel_load_gamma<NP>(P, pp, sm, lane, A);
-            if (npix >= 0) {
-                rows_from_smem<float, NP>(cp, A, lane);
+            const int npix = pixel_load_gamma<NP, false>(P, pp, sm, lane, A);
+            if (npix >= 0 && rows_coherence<NP>(P, pp, A, sm, cp, lane))
                 pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
-            }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();

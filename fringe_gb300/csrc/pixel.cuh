@@ -449,6 +449,72 @@ __device__ bool warp_sweep_inverse(T *A, int n, T *rowk, T *inf_norm, int lane)
     return true;
 }
 
+// The same sweep for FP32 and NP <= 32 with each lane's row in registers:
+// at step k lane k publishes its row (which is also column k) to a shared
+// buffer and every lane updates its own row from it, so the matrix is read
+// from shared memory once and written back once instead of at every step.
+// The arithmetic and its order are those of warp_sweep_inverse.  rowb: 2 x NP
+// floats of shared memory (16-byte aligned).
+template <int LD, int NP>
+__device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf_norm, int lane)
+{
+    static_assert(NP <= 32 && NP % 8 == 0, "one row per lane");
+    float x[NP];
+#pragma unroll
+    for (int j = 0; j < NP; ++j) x[j] = (lane < n && j < n) ? A[lane * LD + j] : 0.f;
+    for (int k = 0; k < n; ++k) {
+        float *rk = rowb + (k & 1) * NP;
+        if (lane == k) {
+#pragma unroll
+            for (int j = 0; j < NP; j += 4) *reinterpret_cast<float4 *>(rk + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+        }
+        __syncwarp();
+        const float p = rk[k];
+        if (!(p > 0.f)) return false;
+        const float rp = 1.f / p;
+        const bool own = (lane == k);
+        // row k: a_kj / p;  other rows: a_ij - (a_ik / p) a_kj  (a_ik = a_ki)
+        const float f = ((lane < NP) ? rk[lane] : 0.f) * rp;
+        const float am = own ? 0.f : 1.f;
+        const float bm = own ? rp : -f;
+#pragma unroll
+        for (int j = 0; j < NP; j += 4) {
+            const float4 r = *reinterpret_cast<const float4 *>(rk + j);
+            x[j] = fmaf(bm, r.x, am * x[j]);
+            x[j + 1] = fmaf(bm, r.y, am * x[j + 1]);
+            x[j + 2] = fmaf(bm, r.z, am * x[j + 2]);
+            x[j + 3] = fmaf(bm, r.w, am * x[j + 3]);
+        }
+        // column k: x[k] = own ? -1/p : a_ik / p (k is a loop variable, so
+        // the register is chosen by block of 8)
+        const float vk = own ? -rp : f;
+        const int kb = k >> 3, ku = k & 7;
+#pragma unroll
+        for (int b = 0; b < NP / 8; ++b) {
+            if (kb == b) {
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (ku == u) x[8 * b + u] = vk;
+            }
+        }
+    }
+    __syncwarp();
+    float s = 0.f;
+    if (lane < n) {
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+            if (j < n) {
+                const float v = -x[j];
+                A[lane * LD + j] = v;
+                s += fabsf(v);
+            }
+        }
+    }
+    *inf_norm = warp_max(s);
+    __syncwarp();
+    return true;
+}
+
 // ------------------------------------------------------------------------
 // Householder tridiagonalisation (restates the zhetd2/zlarfg reduction):
 // Q^H A Q = T, Q = H(0)..H(n-2), reflector v_k in A[k+1.., k] (v_k[0] = 1),
@@ -1213,7 +1279,12 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         const T anorm = warp_max(rs);          // |C| inf-norm
         __syncwarp();
         T xnorm;
-        bool ok = warp_sweep_inverse<T, LD, NP>(Xr, nn, yv, &xnorm, lane);
+        bool ok;
+        if constexpr (sizeof(T) == 4 && NP <= 32)
+            ok = warp_sweep_inverse_rows<LD, NP>(reinterpret_cast<float *>(Xr), nn,
+                                                  reinterpret_cast<float *>(sm + L::wk), &xnorm, lane);
+        else
+            ok = warp_sweep_inverse<T, LD, NP>(Xr, nn, yv, &xnorm, lane);
         if (!fp32) return ok ? 1 : -1;
         if (!ok) return 0;                     // FP32 pivot failure: settle in FP64
         if (!(anorm * xnorm <= T(P.cond_max))) return 0;
@@ -1527,7 +1598,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
 // upper triangle of pairs, holds Re, Im of Gamma_ij for (i, j) = (2a,2b),
 // (2a,2b+1), (2a+1,2b), (2a+1,2b+1).  Returns the SHP count, or -1 when the
 // pixel is finished (or handed to the FP64 path).
-template <int NP>
+template <int NP, bool NORMALIZE = true>
 __device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *sm, int lane, C2<float> *Cm)
 {
     using L = Lay<float, NP>;
@@ -1550,40 +1621,85 @@ __device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *s
         return -1;
     }
     const float *rec = reinterpret_cast<const float *>(P.cbuf) + loc * (long long)P.cstride;
-    const int dp = (n + 1) >> 1;
-    int base = 0;                                   // first block of pair row a
-    for (int a = 0; a < dp; ++a) {
-        for (int b = a + lane; b < dp; b += 32) {
-            const float4 *blk = reinterpret_cast<const float4 *>(rec + 8 * (base + b - a));
-            const float4 u = blk[0], v = blk[1];
-            const int i0 = 2 * a, i1 = 2 * a + 1, j0 = 2 * b, j1 = 2 * b + 1;
-            if (j0 < n) Cm[i0 * LD + j0] = cmk<float>(u.x, u.y);
-            if (j1 < n) Cm[i0 * LD + j1] = cmk<float>(u.z, u.w);
-            if (i1 < n && j0 >= i1) Cm[i1 * LD + j0] = cmk<float>(v.x, v.y);
-            if (j1 < n) Cm[i1 * LD + j1] = cmk<float>(v.z, v.w);
-        }
-        base += dp - a;
+    const int dp = (n + 1) >> 1, nblk = dp * (dp + 1) / 2;
+    // blocks t = 0 .. nblk-1, row-major over the upper triangle of pairs:
+    // pair row a holds blocks (a, a) .. (a, dp-1)
+    for (int t = lane; t < nblk; t += 32) {
+        int a = 0, rem = t;
+        while (rem >= dp - a) { rem -= dp - a; ++a; }
+        const int b = a + rem;
+        const float4 *blk = reinterpret_cast<const float4 *>(rec + 8 * t);
+        const float4 u = __ldg(blk), v = __ldg(blk + 1);
+        const int i0 = 2 * a, i1 = 2 * a + 1, j0 = 2 * b, j1 = 2 * b + 1;
+        if (j0 < n) Cm[i0 * LD + j0] = cmk<float>(u.x, u.y);
+        if (j1 < n) Cm[i0 * LD + j1] = cmk<float>(u.z, u.w);
+        if (i1 < n && j0 >= i1) Cm[i1 * LD + j0] = cmk<float>(v.x, v.y);
+        if (j1 < n) Cm[i1 * LD + j1] = cmk<float>(v.z, v.w);
     }
     __syncwarp();
+    if (!NORMALIZE) return info;
     return gamma_to_coherence<float, NP>(P, pp, Cm, sm, lane) ? info : -1;
 }
 
-// rows of the shared-memory matrix A into the row policy cp
-template <typename T, int NP, typename CP>
-__device__ void rows_from_smem(const CP &cp, const C2<T> *A, int lane)
+// Gamma (upper triangle and diagonal of G, ld NP+1) to coherence rows in
+// the row policy cp, for NP <= 32 (one row per lane): the rule of
+// gamma_to_coherence (C_ij = Gamma_ij / sqrt(P_i P_j) scaled in the same
+// order, lower triangle by conjugation, unit diagonal), with rows and
+// columns >= n set to zero.  Returns false (and writes the failure code)
+// when a result is not finite.
+template <int NP, typename CP>
+__device__ bool rows_coherence(const KParams &P, long long pp, const C2<float> *G, unsigned char *sm,
+                               const CP &cp, int lane)
 {
-#pragma unroll
-    for (int h = 0; h < RowShape<NP>::H; ++h) {
-        const int i = lane + 32 * h;
-#pragma unroll 1
-        for (int c = 0; c < RowShape<NP>::CH; ++c) {
-            C2<T> v[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) v[k] = (i < NP) ? A[i * (NP + 1) + 8 * c + k] : cmk<T>(T(0), T(0));
-            cp.store(h, c, v);
-        }
+    static_assert(NP <= 32 && NP % 8 == 0, "one row per lane");
+    constexpr int LD = NP + 1;
+    float *yv = reinterpret_cast<float *>(sm + Lay<float, NP>::yy);
+    const int n = P.nb;
+    bool bad = false;
+    if (lane < n) {
+        const float Pi = G[lane * LD + lane].x;
+        bad = !(Pi > 0.f) || !isfinite(Pi);
+        yv[lane] = 1.f / sqrtf(Pi);
     }
-    cp.fence();
+    bad = __any_sync(0xffffffffu, bad);
+    __syncwarp();
+    if (!bad) {
+        const float ri = (lane < n) ? yv[lane] : 0.f;
+#pragma unroll 1
+        for (int c = 0; c < NP / 8; ++c) {
+            const float4 ya = *reinterpret_cast<const float4 *>(yv + 8 * c);
+            const float4 yb = *reinterpret_cast<const float4 *>(yv + 8 * c + 4);
+            const float yj[8] = {ya.x, ya.y, ya.z, ya.w, yb.x, yb.y, yb.z, yb.w};
+            C2<float> v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int j = 8 * c + k;
+                C2<float> e = cmk<float>(0.f, 0.f);
+                if (lane < n && j < n) {
+                    if (j > lane) {
+                        e = cscale(G[lane * LD + j], ri * yj[k]);
+                    } else if (j < lane) {
+                        // the conjugate of row j's entry, scaled in its order
+                        e = cconj(cscale(G[j * LD + lane], yj[k] * ri));
+                    } else {
+                        e = cmk<float>(1.f, 0.f);
+                    }
+                    bad |= !isfinite(e.x) || !isfinite(e.y);
+                }
+                v[k] = e;
+            }
+            cp.store(0, c, v);
+        }
+        cp.fence();
+        bad = __any_sync(0xffffffffu, bad);
+    }
+    __syncwarp();
+    if (bad) {
+        // non-finite coherence: the first eigen call is reported as failed
+        put_code(P, pp, lane, (P.semantics != SEM_PL && P.method != M_MLE) ? -6 : -1);
+        return false;
+    }
+    return true;
 }
 
 template <typename T, int NP>
