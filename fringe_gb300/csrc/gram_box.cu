@@ -297,6 +297,48 @@ __global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
         }
         // (the first chunk's barriers order these before any use)
 
+        // samples of chunk k0 (date pairs interleaved): each thread loads one
+        // sample for up to BX_XPT dates into registers; put() stores them in
+        // Xb and flags samples outside the split range for the stage's mask
+        constexpr int BX_XPT = 8;
+        const int sidx = tid % KC, d0 = tid / KC;
+        float2 xv[BX_XPT];
+        bool xbad = false;
+        auto fetch = [&](int k0) {
+            const int k = k0 + sidx;
+            const int ur = k / uwp, uc = k - ur * uwp;
+            const int r = R0 - P.ny + ur, c = C0 - P.nx + uc;
+            const bool valid = uc < uw && ur < uh && r >= 0 && r < rows && c >= 0 && c < cols;
+            const float2 *src = P.stack + (valid ? (long long)r * cols + c : 0ll);
+            xbad = false;
+#pragma unroll
+            for (int q = 0; q < BX_XPT; ++q) {
+                const int d = d0 + q * (BX_THREADS / KC);
+                float2 x = make_float2(0.f, 0.f);
+                if (valid && d < n) x = __ldg(src + d * plane);
+                xv[q] = x;
+            }
+        };
+        auto put = [&](uint32_t *bw) {
+#pragma unroll
+            for (int q = 0; q < BX_XPT; ++q) {
+                const int d = d0 + q * (BX_THREADS / KC);
+                if (d >= 2 * dp) break;
+                float2 x = xv[q];
+                if (!split_range(x.x) || !split_range(x.y)) {
+                    xbad = true;
+                    x = make_float2(0.f, 0.f);
+                }
+                *reinterpret_cast<float2 *>(Xb + (d >> 1) * L::XRS + sidx * 16 + (d & 1) * 8) = x;
+            }
+            if (xbad) atomicOr(bw + (sidx >> 5), 1u << (sidx & 31));
+        };
+        // prologue: the first chunk of the tile into Xb (its stage's flags
+        // were cleared when that stage was last used, or at start-up)
+        fetch(0);
+        put(badw + (gstep & 1) * (KC / 32));
+        __syncthreads();
+
         for (int pass = 0; pass < npass && !timed_out; ++pass) {
             const int cb = pass * BX_NCOL;
             const int ncol = min(BX_NCOL, ncolt - cb);
@@ -309,30 +351,11 @@ __global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
                 unsigned char *Bh = As + L::A_BYTES, *Bl = Bh + L::B_BYTES;
                 uint32_t *bw = badw + s * (KC / 32);
                 const int k0 = ch * KC;
-                // ---- samples of the chunk, date pairs interleaved ----
-                {
-                    const int sidx = tid % KC;
-                    const int k = k0 + sidx;
-                    const int ur = k / uwp, uc = k - ur * uwp;
-                    const int r = R0 - P.ny + ur, c = C0 - P.nx + uc;
-                    const bool valid = uc < uw && ur < uh && r >= 0 && r < rows && c >= 0 && c < cols;
-                    const float2 *src = P.stack + (valid ? (long long)r * cols + c : 0ll);
-                    bool bad = false;
-                    for (int d = tid / KC; d < 2 * dp; d += BX_THREADS / KC) {
-                        float2 x = make_float2(0.f, 0.f);
-                        if (valid && d < n) {
-                            x = __ldg(src + d * plane);
-                            if (!split_range(x.x) || !split_range(x.y)) {
-                                bad = true;
-                                x = make_float2(0.f, 0.f);
-                            }
-                        }
-                        *reinterpret_cast<float2 *>(Xb + (d >> 1) * L::XRS + sidx * 16 + (d & 1) * 8) = x;
-                    }
-                    if (bad) atomicOr(bw + (sidx >> 5), 1u << (sidx & 31));
-                }
+                // the next chunk (the first chunk again after the last one of
+                // a pass) is loaded while this one is built
+                const bool more = (ch + 1 < nchunk) || (pass + 1 < npass);
+                if (more) fetch(ch + 1 < nchunk ? k0 + KC : 0);
                 if (tid < KC / 32) badw[(s ^ 1) * (KC / 32) + tid] = 0;   // for the next chunk
-                __syncthreads();
                 // ---- A: SHP mask rows ----
                 for (int e = tid; e < BX_M * (KC / 8); e += BX_THREADS) {
                     const int m = e & (BX_M - 1), k8 = e >> 7;
@@ -407,6 +430,10 @@ __global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
                 }
                 pend |= 1u << s;
                 ++gstep;
+                // every thread has finished building this chunk (barrier
+                // above): the prefetched samples replace it in Xb; the next
+                // iteration's wait is the barrier before they are read
+                if (more) put(badw + (s ^ 1) * (KC / 32));
             }
             if (timed_out) break;
             if (!wait_stage(0) || !wait_stage(1)) { timed_out = true; break; }
