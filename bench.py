@@ -163,12 +163,12 @@ def cpu_baseline(stack, nmap, method, rows):
 
 def serving_measurement(njobs, seed=5):
     """Serving loop on a mix of jobs: tiles 256^2..1024^2, N in 10..60,
-    half-windows 3x3..5x10, MLE/EVD.  (1) all jobs submitted at once
-    (saturating load): throughput and p50/p99 latency; (2) Poisson arrivals
-    at 70% of the saturated job rate: p50/p99 latency."""
+    half-windows 3x3..5x10, MLE/EVD, in the mixed-precision form and in the
+    plain FP32 form.  Per form: (1) all jobs submitted at once (saturating
+    load): throughput and p50/p99 latency; (2) Poisson arrivals at 70% of
+    the saturated job rate: p50/p99 latency."""
     from fringe_gb300 import synth
     from fringe_gb300.serve import Server
-    rng = np.random.Generator(np.random.PCG64(seed))
     shapes = [(256, 10, (3, 3)), (512, 30, (5, 10)), (1024, 20, (3, 5)), (512, 60, (5, 10)),
               (256, 45, (4, 8)), (1024, 30, (5, 10))]
     import torch
@@ -180,7 +180,6 @@ def serving_measurement(njobs, seed=5):
     for k, (r, n, hw) in enumerate(shapes):
         st, nm = synth.scene("voronoi", r, r, n, hw[0], hw[1], seed=100 + k)
         pool.append((pinned(st), pinned(nm.view(np.int32)).view(np.uint32), hw))
-    picks = rng.integers(0, len(pool), njobs)
 
     def outputs(p):
         nb, R, C = pool[p][0].shape
@@ -188,42 +187,48 @@ def serving_measurement(njobs, seed=5):
                 "tcorr": torch.zeros((R, C), dtype=torch.float32).pin_memory().numpy(),
                 "comp": torch.zeros((R, C), dtype=torch.complex64).pin_memory().numpy()}
 
-    outs = [outputs(p) for p in picks]
-    methods = rng.choice(["MLE", "EVD"], njobs)
-    srv = Server(memory_budget=80 << 30, wave_pixels=1 << 19)
-    # warm-up (kernel loading, allocator)
-    st, nm, hw = pool[0]
-    srv.wait(srv.submit(st, nm, hw))
+    result = {"jobs": int(njobs),
+              "mix": "tiles 256^2..1024^2, N 10..60, half-windows 3x3..5x10, MLE/EVD, 80 GB budget"}
+    for prec in ("mixed", "fp32"):
+        rng = np.random.Generator(np.random.PCG64(seed))
+        picks = rng.integers(0, len(pool), njobs)
+        outs = [outputs(p) for p in picks]
+        methods = rng.choice(["MLE", "EVD"], njobs)
+        srv = Server(memory_budget=80 << 30, wave_pixels=1 << 19)
+        # warm-up (kernel loading, allocator)
+        st, nm, hw = pool[0]
+        srv.wait(srv.submit(st, nm, hw, precision=prec))
 
-    def run(arrivals):
-        t0 = time.perf_counter()
-        tickets = []
-        for k in range(njobs):
-            if arrivals is not None:
-                dt = arrivals[k] - (time.perf_counter() - t0)
-                if dt > 0:
-                    time.sleep(dt)
-            st, nm, hw = pool[picks[k]]
-            tickets.append(srv.submit(st, nm, hw, method=str(methods[k]), out=outs[k]))
-        lat = [srv.wait(t)["total_ms"] for t in tickets]
-        wall = time.perf_counter() - t0
-        for t in tickets:
-            srv.result(t)
-        return wall, np.array(lat)
+        def run(arrivals):
+            t0 = time.perf_counter()
+            tickets = []
+            for k in range(njobs):
+                if arrivals is not None:
+                    dt = arrivals[k] - (time.perf_counter() - t0)
+                    if dt > 0:
+                        time.sleep(dt)
+                st, nm, hw = pool[picks[k]]
+                tickets.append(srv.submit(st, nm, hw, method=str(methods[k]), out=outs[k], precision=prec))
+            lat = [srv.wait(t)["total_ms"] for t in tickets]
+            wall = time.perf_counter() - t0
+            for t in tickets:
+                srv.result(t)
+            return wall, np.array(lat)
 
-    px = float(sum(pool[p][0].shape[1] * pool[p][0].shape[2] for p in picks))
-    wall, lat = run(None)
-    rate_sat = njobs / wall
-    rate = 0.7 * rate_sat
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs))
-    _, lat_p = run(arrivals)
-    srv.close()
-    return {"jobs": int(njobs), "pixels": px,
+        px = float(sum(pool[p][0].shape[1] * pool[p][0].shape[2] for p in picks))
+        wall, lat = run(None)
+        rate_sat = njobs / wall
+        rate = 0.7 * rate_sat
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs))
+        _, lat_p = run(arrivals)
+        srv.close()
+        result["pixels"] = px
+        result[prec] = {
             "saturated": {"throughput_px_s": px / wall, "jobs_per_s": rate_sat,
                           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
             "poisson": {"rate_jobs_per_s": rate, "p50_ms": float(np.percentile(lat_p, 50)),
-                        "p99_ms": float(np.percentile(lat_p, 99))},
-            "mix": "tiles 256^2..1024^2, N 10..60, half-windows 3x3..5x10, MLE/EVD, 80 GB budget"}
+                        "p99_ms": float(np.percentile(lat_p, 99))}}
+    return result
 
 
 def run_reference(args, rank):

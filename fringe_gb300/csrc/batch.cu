@@ -10,6 +10,13 @@
 // (counter resets and the kernels of every depth class) can be captured once
 // into a CUDA graph and replayed.
 //
+// Jobs in the mixed-precision form (fpl_job::precision = FPL_PREC_MIXED) are
+// cut into row pieces and packed into waves of at most 2^20 pixels; a wave
+// is one persistent tensor-core Gamma launch over the tiles of all its
+// pieces (per sample-chunk width) and one persistent solve launch over all
+// its pixels (per padded depth), the Gamma records staying in a buffer
+// sized for one wave.  Their FP64 settle runs with the FP32 jobs' at the end.
+//
 // An optional autotuner times the candidate CTA shapes (warps per CTA) of
 // each depth class on the batch itself and keeps the fastest per
 // (NP, window taps, mean SHP count) key in the context.
@@ -224,9 +231,26 @@ struct BatchClass {
     int warps = 0;                  // CTA shape
 };
 
+// one wave of the mixed-form pieces: Gamma segments per chunk width
+// (index 0: 64 samples, 1: 32) and solve entries per padded depth (16/32/64)
+struct MixedWave {
+    int seg_first[2] = {0, 0}, seg_count[2] = {0, 0};
+    long long seg_tiles[2] = {0, 0};
+    size_t seg_smem[2] = {0, 0};
+    int ent_first[3] = {0, 0, 0}, ent_count[3] = {0, 0, 0};
+    long long ent_total[3] = {0, 0, 0};
+};
+
 struct fpl_batch {
     fpl_ctx *ctx = nullptr;
     int njobs = 0;
+    int nent = 0;                    // counter blocks: FP32 jobs, then mixed pieces
+    std::vector<MixedWave> waves;
+    fpl::BoxSeg *d_segs = nullptr;   // mixed: Gamma segments of every wave
+    fpl::BatchEntry *d_ments = nullptr;   // mixed: solve entries of every wave
+    fpl::BatchEntry *d_m64 = nullptr;     // mixed: every piece, by padded depth (FP64 settle)
+    int m64_first[3] = {0, 0, 0}, m64_count[3] = {0, 0, 0};
+    void *d_rec = nullptr;           // mixed: Gamma records and tile infos of one wave
     std::vector<BatchClass> classes;
     fpl::BatchEntry *d_table = nullptr;
     void *d_scratch = nullptr;       // per-job counters, work counters, FP64 lists
@@ -254,8 +278,25 @@ int batch_enqueue(fpl_batch *b, cudaStream_t st)
             cudaSuccess)
             return FPL_ERR_CUDA;
     }
+    static const int kKC[2] = {64, 32};
+    static const int kNP[3] = {16, 32, 64};
+    for (const MixedWave &w : b->waves) {
+        for (int c = 0; c < 2; ++c)
+            if (w.seg_count[c] && fpl::launch_gram_batch(kKC[c], b->d_segs + w.seg_first[c], w.seg_count[c],
+                                                         w.seg_tiles[c], w.seg_smem[c], ctx->num_sms,
+                                                         st) != cudaSuccess)
+                return FPL_ERR_CUDA;
+        for (int c = 0; c < 3; ++c)
+            if (w.ent_count[c] && fpl::launch_solve_batch(kNP[c], b->d_ments + w.ent_first[c], w.ent_count[c],
+                                                          w.ent_total[c], ctx->num_sms, st) != cudaSuccess)
+                return FPL_ERR_CUDA;
+    }
     for (const BatchClass &k : b->classes)
         if (fpl::launch_batch64(k.np, b->d_table + k.first, k.count, ctx->num_sms, st) != cudaSuccess)
+            return FPL_ERR_CUDA;
+    for (int c = 0; c < 3; ++c)
+        if (b->m64_count[c] &&
+            fpl::launch_batch64(kNP[c], b->d_m64 + b->m64_first[c], b->m64_count[c], ctx->num_sms, st) != cudaSuccess)
             return FPL_ERR_CUDA;
     return FPL_OK;
 }
@@ -273,6 +314,10 @@ int fpl_batch_destroy(fpl_batch *b)
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     if (b->d_table) cudaFree(b->d_table);
     if (b->d_scratch) cudaFree(b->d_scratch);
+    if (b->d_segs) cudaFree(b->d_segs);
+    if (b->d_ments) cudaFree(b->d_ments);
+    if (b->d_m64) cudaFree(b->d_m64);
+    if (b->d_rec) cudaFree(b->d_rec);
     delete b;
     return FPL_OK;
 }
@@ -290,11 +335,32 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
     fpl_batch *b = new fpl_batch();
     b->ctx = ctx;
     b->njobs = njobs;
-    // group by padded depth
-    std::vector<int> order(njobs);
-    for (int j = 0; j < njobs; ++j) order[j] = j;
+    auto is_mixed = [&](const fpl_job &jb) {
+        return jb.precision == FPL_PREC_MIXED && fpl::gram_box_supported(jb.nbands, jb.half_window_y, jb.half_window_x);
+    };
+    // FP32 jobs, grouped by padded depth
+    std::vector<int> order;
+    for (int j = 0; j < njobs; ++j)
+        if (!is_mixed(jobs[j])) order.push_back(j);
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int c) { return fpl::pick_np(jobs[a].nbands) < fpl::pick_np(jobs[c].nbands); });
+    const int nf = (int)order.size();
+    // mixed jobs: row pieces of at most kWavePx pixels, packed into waves
+    struct Piece { int job, ra, rb; long long px; };
+    const long long kWavePx = 1ll << 20;
+    std::vector<Piece> pieces;
+    for (int j = 0; j < njobs; ++j) {
+        if (!is_mixed(jobs[j])) continue;
+        const fpl_job &jb = jobs[j];
+        const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
+        const int step = (int)std::max<long long>(1, kWavePx / jb.cols);
+        for (int ra = r0; ra < r1; ra += step) {
+            const int rb = std::min(r1, ra + step);
+            pieces.push_back({j, ra, rb, (long long)(rb - ra) * jb.cols});
+        }
+    }
+    const int np_ = (int)pieces.size();
+    b->nent = nf + np_;
     long long fb_total = 0;
     for (int j = 0; j < njobs; ++j) {
         const fpl_job &jb = jobs[j];
@@ -302,35 +368,148 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
         fb_total += (long long)(r1 - jb.row_begin) * jb.cols;
     }
     b->pixels = fb_total;
-    // scratch: per-job counters | work counters (one per class, <= 3) | FP64 lists
-    b->counter_bytes = kJobCounterBytes * njobs + 64;
+    // scratch: per-entry counters | work counters (one per class, <= 3) | FP64 lists
+    b->counter_bytes = kJobCounterBytes * b->nent + 64;
     const size_t scratch = b->counter_bytes + sizeof(long long) * (size_t)std::max<long long>(fb_total, 1);
     if (cudaMalloc(&b->d_scratch, scratch) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_NOMEM; }
-    std::vector<fpl::BatchEntry> table(njobs);
+    std::vector<fpl::BatchEntry> table(nf);
     long long fb_off = 0;
     char *cnt_base = static_cast<char *>(b->d_scratch);
     long long *lists = reinterpret_cast<long long *>(cnt_base + b->counter_bytes);
-    for (int e = 0; e < njobs; ++e) {
-        const int j = order[e];
-        const fpl_job &jb = jobs[j];
-        const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
-        fpl::KParams &P = table[e].P;
-        fpl::fill_params(P, jb, r0, r1, ctx->amb_scale, ctx->cond_max);
+    auto set_counters = [&](fpl::KParams &P, int e) {
         P.fb_count = reinterpret_cast<int *>(cnt_base + kJobCounterBytes * e);
         P.err = reinterpret_cast<unsigned *>(cnt_base + kJobCounterBytes * e + 16);
         P.slow = reinterpret_cast<int *>(cnt_base + kJobCounterBytes * e + 32);
         P.fb_list = lists + fb_off;
         P.fb_cap = (int)std::min<long long>(P.npix, 0x7fffffff);
         fb_off += P.npix;
+    };
+    for (int e = 0; e < nf; ++e) {
+        const int j = order[e];
+        const fpl_job &jb = jobs[j];
+        const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
+        fpl::KParams &P = table[e].P;
+        fpl::fill_params(P, jb, r0, r1, ctx->amb_scale, ctx->cond_max);
+        set_counters(P, e);
         b->job_of_entry.push_back(j);
     }
+    // mixed pieces: parameters, waves, records buffer
+    if (np_ > 0) {
+        std::vector<fpl::KParams> pp(np_);
+        std::vector<int> wave_of(np_);
+        std::vector<long long> rec_off(np_), info_off(np_);
+        size_t rec_max = 0, info_max = 0;
+        {
+            long long wpx = 0;
+            size_t rec = 0, inf = 0;
+            int w = -1;
+            for (int i = 0; i < np_; ++i) {
+                const Piece &pc = pieces[i];
+                const fpl_job &jb = jobs[pc.job];
+                if (w < 0 || wpx + pc.px > kWavePx) { ++w; wpx = 0; rec = 0; inf = 0; }
+                wave_of[i] = w;
+                wpx += pc.px;
+                const int cstride = fpl::gram_box_record(jb.nbands);
+                rec_off[i] = (long long)rec;
+                info_off[i] = (long long)inf;
+                rec += (size_t)pc.px * cstride;
+                inf += (size_t)pc.px;
+                rec_max = std::max(rec_max, rec);
+                info_max = std::max(info_max, inf);
+            }
+            b->waves.resize(w + 1);
+        }
+        const size_t rec_bytes = (sizeof(float) * rec_max + 255) & ~size_t(255);
+        if (cudaMalloc(&b->d_rec, rec_bytes + sizeof(int) * std::max<size_t>(info_max, 1)) != cudaSuccess) {
+            fpl_batch_destroy(b);
+            return FPL_ERR_NOMEM;
+        }
+        float *recs = static_cast<float *>(b->d_rec);
+        int *infos = reinterpret_cast<int *>(static_cast<char *>(b->d_rec) + rec_bytes);
+        for (int i = 0; i < np_; ++i) {
+            const Piece &pc = pieces[i];
+            const fpl_job &jb = jobs[pc.job];
+            fpl::KParams &P = pp[i];
+            fpl::fill_params(P, jb, pc.ra, pc.rb, ctx->amb_scale, ctx->cond_max);
+            set_counters(P, nf + i);
+            P.cbuf = reinterpret_cast<float2 *>(recs + rec_off[i]);
+            P.cinfo = infos + info_off[i];
+            P.cbase = P.pix_begin;
+            P.cstride = fpl::gram_box_record(jb.nbands);
+            b->job_of_entry.push_back(pc.job);
+        }
+        // per wave: segments by chunk width, entries by padded depth
+        std::vector<fpl::BoxSeg> segs;
+        std::vector<fpl::BatchEntry> ments;
+        for (size_t w = 0; w < b->waves.size(); ++w) {
+            MixedWave &mw = b->waves[w];
+            for (int c = 0; c < 2; ++c) {
+                const int kc = c == 0 ? 64 : 32;
+                mw.seg_first[c] = (int)segs.size();
+                for (int i = 0; i < np_; ++i) {
+                    if (wave_of[i] != (int)w || fpl::gram_box_kc(pp[i].nb) != kc) continue;
+                    fpl::BoxSeg sg;
+                    sg.P = pp[i];
+                    sg.tile_offset = mw.seg_tiles[c];
+                    mw.seg_tiles[c] += fpl::gram_box_tiles(pp[i]);
+                    mw.seg_smem[c] = std::max(mw.seg_smem[c], fpl::gram_box_smem(pp[i].nb, pp[i].ny, pp[i].nx));
+                    segs.push_back(sg);
+                }
+                mw.seg_count[c] = (int)segs.size() - mw.seg_first[c];
+            }
+            for (int c = 0; c < 3; ++c) {
+                const int npd = 16 << c;
+                mw.ent_first[c] = (int)ments.size();
+                for (int i = 0; i < np_; ++i) {
+                    if (wave_of[i] != (int)w || fpl::pick_np(pp[i].nb) != npd) continue;
+                    fpl::BatchEntry en;
+                    en.P = pp[i];
+                    en.px_offset = mw.ent_total[c];
+                    mw.ent_total[c] += pp[i].npix;
+                    ments.push_back(en);
+                }
+                mw.ent_count[c] = (int)ments.size() - mw.ent_first[c];
+            }
+        }
+        // FP64 settle table: every piece, by padded depth
+        std::vector<fpl::BatchEntry> m64;
+        for (int c = 0; c < 3; ++c) {
+            const int npd = 16 << c;
+            b->m64_first[c] = (int)m64.size();
+            for (int i = 0; i < np_; ++i) {
+                if (fpl::pick_np(pp[i].nb) != npd) continue;
+                fpl::BatchEntry en;
+                en.P = pp[i];
+                en.px_offset = 0;
+                m64.push_back(en);
+            }
+            b->m64_count[c] = (int)m64.size() - b->m64_first[c];
+            if (b->m64_count[c] && fpl::configure_np(npd) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
+        }
+        if (cudaMalloc(&b->d_segs, sizeof(fpl::BoxSeg) * std::max<size_t>(segs.size(), 1)) != cudaSuccess ||
+            cudaMalloc(&b->d_ments, sizeof(fpl::BatchEntry) * std::max<size_t>(ments.size(), 1)) != cudaSuccess ||
+            cudaMalloc(&b->d_m64, sizeof(fpl::BatchEntry) * std::max<size_t>(m64.size(), 1)) != cudaSuccess) {
+            fpl_batch_destroy(b);
+            return FPL_ERR_NOMEM;
+        }
+        if (cudaMemcpy(b->d_segs, segs.data(), sizeof(fpl::BoxSeg) * segs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->d_ments, ments.data(), sizeof(fpl::BatchEntry) * ments.size(), cudaMemcpyHostToDevice) !=
+                cudaSuccess ||
+            cudaMemcpy(b->d_m64, m64.data(), sizeof(fpl::BatchEntry) * m64.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            fpl_batch_destroy(b);
+            return FPL_ERR_CUDA;
+        }
+        // kernel attributes are set before any capture
+        for (int c = 0; c < 3; ++c)
+            if (fpl::prepare_mixed_batch(16 << c) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
+    }
     // classes and their pixel offsets
-    for (int e = 0; e < njobs;) {
+    for (int e = 0; e < nf;) {
         BatchClass k;
         k.np = fpl::pick_np(table[e].P.nb);
         k.first = e;
         long long off = 0;
-        while (e < njobs && fpl::pick_np(table[e].P.nb) == k.np) {
+        while (e < nf && fpl::pick_np(table[e].P.nb) == k.np) {
             table[e].px_offset = off;
             off += table[e].P.npix;
             ++e;
@@ -341,11 +520,11 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
         if (fpl::configure_np(k.np) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
         b->classes.push_back(k);
     }
-    if (cudaMalloc(&b->d_table, sizeof(fpl::BatchEntry) * njobs) != cudaSuccess) {
+    if (cudaMalloc(&b->d_table, sizeof(fpl::BatchEntry) * std::max(nf, 1)) != cudaSuccess) {
         fpl_batch_destroy(b);
         return FPL_ERR_NOMEM;
     }
-    if (cudaMemcpy(b->d_table, table.data(), sizeof(fpl::BatchEntry) * njobs, cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (nf && cudaMemcpy(b->d_table, table.data(), sizeof(fpl::BatchEntry) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
         fpl_batch_destroy(b);
         return FPL_ERR_CUDA;
     }
@@ -438,7 +617,7 @@ int fpl_batch_stats(const fpl_batch *b, fpl_stats *out)
     std::memset(out, 0, sizeof(*out));
     out->pixels = b->pixels;
     unsigned err = 0;
-    for (int e = 0; e < b->njobs; ++e) {
+    for (int e = 0; e < b->nent; ++e) {
         out->fp64_pixels += c[(kJobCounterBytes / sizeof(int)) * e];
         err |= (unsigned)c[(kJobCounterBytes / sizeof(int)) * e + 4];
         out->slow_path_pixels += c[(kJobCounterBytes / sizeof(int)) * e + 8];

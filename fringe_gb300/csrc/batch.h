@@ -9,11 +9,6 @@
 
 namespace fpl {
 
-struct BatchEntry {
-    KParams P;
-    long long px_offset;   // first pixel of this job in the class's concatenated range
-};
-
 // warps per CTA that fit the shared-memory budget for a padded depth
 int max_warps(int np, bool fp64);
 // function attributes (dynamic shared memory, carveout) of the batch kernels

@@ -179,15 +179,51 @@ __device__ __forceinline__ void store_split(unsigned char *dh, unsigned char *dl
     *reinterpret_cast<uint4 *>(dl) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// pipeline state of a CTA, carried from tile to tile (and job to job)
+struct BoxPipe {
+    uint32_t pend;      // per stage: MMAs in flight
+    uint32_t par;       // per stage: mbarrier parity
+    unsigned gstep;     // chunks issued
+    bool timed_out;
+    int blk_dp;         // date pairs the block table was built for
+};
+
+// wait until the MMAs reading stage s are complete; the vote keeps the
+// timeout decision uniform across the CTA
+__device__ __forceinline__ bool box_wait(uint64_t *mbar, BoxPipe &st, int s)
+{
+    bool late = false;
+    if (st.pend & (1u << s)) {
+        long long spins = 0;
+        while (!mbar_try_wait(&mbar[s], (st.par >> s) & 1u)) {
+            if (++spins > BX_SPIN_LIMIT) { late = true; break; }
+        }
+        if (!late) { st.par ^= 1u << s; st.pend &= ~(1u << s); }
+    }
+    return __syncthreads_or(late) == 0;
+}
+
+// tiles of the rows [ra, rb) of a launch: 8-row tiles on the absolute grid
+// (rows 8t .. 8t+7 of the scene) so that a pixel's Gamma, and its order of
+// accumulation, do not depend on how the rows were split into launches
+__device__ __forceinline__ int box_first_row(const KParams &P) { return int(P.pix_begin / P.cols) / BX_TR * BX_TR; }
+__host__ __device__ __forceinline__ long long box_tiles(const KParams &P)
+{
+    const int ra = int(P.pix_begin / P.cols), rb = ra + int(P.npix / P.cols);
+    if (rb <= ra) return 0;
+    const int r0 = ra / BX_TR * BX_TR;
+    return (long long)((P.cols + BX_TC - 1) / BX_TC) * ((rb - r0 + BX_TR - 1) / BX_TR);
+}
+
+// Gamma records of tile t of the launch described by P (all threads of the
+// CTA call it together)
 template <int KC>
-__global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
+__device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uint32_t tbase, BoxPipe &st)
 {
     using L = BoxLay<KC>;
-    extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *Xb = smem + L::OFF_X;
     unsigned char *misc = smem + L::OFF_MISC;
     uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);                 // 2 stages
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(misc + 16);
     uint32_t *badw = reinterpret_cast<uint32_t *>(misc + 32);            // [2][KC / 32]
     int *pinfo = reinterpret_cast<int *>(misc + 64);                     // 128
     int *pdefer = reinterpret_cast<int *>(misc + 64 + 512);              // 128
@@ -203,12 +239,259 @@ __global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
     const int kp = (uh * uwp + KC - 1) / KC * KC, nchunk = kp / KC;
     const int W = kp >> 5;
     const int ra = int(P.pix_begin / cols), rb = ra + int(P.npix / cols);
-    const int ntc = (cols + BX_TC - 1) / BX_TC, ntr = (rb - ra + BX_TR - 1) / BX_TR;
-    const long long ntiles = (long long)ntc * ntr;
+    const int ntc = (cols + BX_TC - 1) / BX_TC;
     const int npass = (ncolt + BX_NCOL - 1) / BX_NCOL;
     const int min_neigh = (P.semantics == SEM_PL) ? P.min_neigh : 2;   // evd.cpp:566
     const long long plane = P.plane;
+    const int R0 = box_first_row(P) + int(t / ntc) * BX_TR, C0 = int(t % ntc) * BX_TC;
 
+    // Gamma column blocks (a, b), a <= b, of this stack depth
+    if (st.blk_dp != dp) {
+        __syncthreads();
+        for (int b = tid; b < nblk; b += BX_THREADS) {
+            int a = 0, rem = b;
+            while (rem >= dp - a) { rem -= dp - a; ++a; }
+            blk[b] = make_short2((short)a, (short)(a + rem));
+        }
+        st.blk_dp = dp;
+    }
+    // ---- per-pixel SHP masks over the union samples ----------------
+    for (int e = tid; e < BX_M * W; e += BX_THREADS) umask[e] = 0;
+    for (int e = tid; e < BX_M * nul; e += BX_THREADS) {
+        const int m = e / nul, w = e - m * nul;
+        const int r = R0 + m / BX_TC, c = C0 + m % BX_TC;
+        nm[e] = (r >= ra && r < rb && c < cols) ? __ldg(P.nmap + ((long long)r * cols + c) * nul + w) : 0u;
+    }
+    __syncthreads();
+    for (int e = tid; e < BX_M * wy; e += BX_THREADS) {
+        const int m = e / wy, a = e - m * wy;
+        const int tr = m / BX_TC, tc = m % BX_TC;
+        const int r = R0 + tr, c = C0 + tc;
+        const int sr = r - P.ny + a;                    // image row of window row a
+        if (r < ra || r >= rb || c >= cols || sr < 0 || sr >= rows) continue;
+        uint64_t bits = extract_bits(nm + m * nul, nul, a * wx, wx);
+        // window column b is image column c - nx + b (evd.cpp:530-534)
+        const int blo = max(0, P.nx - c), bhi = min(wx, cols - c + P.nx);
+        if (bhi <= blo) continue;
+        bits &= ((1ull << (bhi - blo)) - 1ull) << blo;
+        if (!bits) continue;
+        const int pos = (tr + a) * uwp + tc;            // union sample of window (a, 0)
+        const int w0 = pos >> 5, sh = pos & 31;
+        const uint64_t lo = bits << sh;
+        const uint32_t hi = sh ? (uint32_t)(bits >> (64 - sh)) : 0u;
+        uint32_t *um = umask + m * W;
+        if ((uint32_t)lo) atomicOr(um + w0, (uint32_t)lo);
+        if ((uint32_t)(lo >> 32)) atomicOr(um + w0 + 1, (uint32_t)(lo >> 32));
+        if (hi) atomicOr(um + w0 + 2, hi);
+    }
+    __syncthreads();
+    if (tid < BX_M) {
+        const int m = tid, r = R0 + m / BX_TC, c = C0 + m % BX_TC;
+        int info = CI_SKIP;                                 // outside rows [ra, rb) of this launch
+        if (r >= ra && r < rb && c < cols) {
+            const int cflat = P.ny * wx + P.nx;
+            if (!((nm[m * nul + (cflat >> 5)] >> (cflat & 31)) & 1u)) {
+                info = CI_CENTRE;                       // evd.cpp:517
+            } else {
+                int cnt = 0;
+                for (int w = 0; w < W; ++w) cnt += __popc(umask[m * W + w]);
+                info = (cnt < min_neigh) ? CI_FEW : cnt;
+            }
+        }
+        pinfo[m] = info;
+        pdefer[m] = 0;
+    }
+    // (the first chunk's barriers order these before any use)
+
+    // samples of chunk k0 (date pairs interleaved): each thread loads one
+    // sample for up to BX_XPT dates into registers; put() stores them in
+    // Xb and flags samples outside the split range for the stage's mask
+    constexpr int BX_XPT = 8;
+    const int sidx = tid % KC, d0 = tid / KC;
+    float2 xv[BX_XPT];
+    bool xbad = false;
+    auto fetch = [&](int k0) {
+        const int k = k0 + sidx;
+        const int ur = k / uwp, uc = k - ur * uwp;
+        const int r = R0 - P.ny + ur, c = C0 - P.nx + uc;
+        const bool valid = uc < uw && ur < uh && r >= 0 && r < rows && c >= 0 && c < cols;
+        const float2 *src = P.stack + (valid ? (long long)r * cols + c : 0ll);
+        xbad = false;
+#pragma unroll
+        for (int q = 0; q < BX_XPT; ++q) {
+            const int d = d0 + q * (BX_THREADS / KC);
+            float2 x = make_float2(0.f, 0.f);
+            if (valid && d < n) x = __ldg(src + d * plane);
+            xv[q] = x;
+        }
+    };
+    auto put = [&](uint32_t *bw) {
+#pragma unroll
+        for (int q = 0; q < BX_XPT; ++q) {
+            const int d = d0 + q * (BX_THREADS / KC);
+            if (d >= 2 * dp) break;
+            float2 x = xv[q];
+            if (!split_range(x.x) || !split_range(x.y)) {
+                xbad = true;
+                x = make_float2(0.f, 0.f);
+            }
+            *reinterpret_cast<float2 *>(Xb + (d >> 1) * L::XRS + sidx * 16 + (d & 1) * 8) = x;
+        }
+        if (xbad) atomicOr(bw + (sidx >> 5), 1u << (sidx & 31));
+    };
+    // prologue: the first chunk of the tile into Xb (its stage's flags
+    // were cleared when that stage was last used, or at start-up)
+    fetch(0);
+    put(badw + (st.gstep & 1) * (KC / 32));
+    __syncthreads();
+
+    for (int pass = 0; pass < npass && !st.timed_out; ++pass) {
+        const int cb = pass * BX_NCOL;
+        const int ncol = min(BX_NCOL, ncolt - cb);
+        const int nmma = (ncol + 15) & ~15;
+        const uint32_t idesc = make_idesc(nmma);
+        for (int ch = 0; ch < nchunk; ++ch) {
+            const int s = st.gstep & 1;
+            if (!box_wait(mbar, st, s)) { st.timed_out = true; break; }
+            unsigned char *As = smem + s * L::STAGE;
+            unsigned char *Bh = As + L::A_BYTES, *Bl = Bh + L::B_BYTES;
+            uint32_t *bw = badw + s * (KC / 32);
+            const int k0 = ch * KC;
+            // the next chunk (the first chunk again after the last one of
+            // a pass) is loaded while this one is built
+            const bool more = (ch + 1 < nchunk) || (pass + 1 < npass);
+            if (more) fetch(ch + 1 < nchunk ? k0 + KC : 0);
+            if (tid < KC / 32) badw[(s ^ 1) * (KC / 32) + tid] = 0;   // for the next chunk
+            // ---- A: SHP mask rows ----
+            for (int e = tid; e < BX_M * (KC / 8); e += BX_THREADS) {
+                const int m = e & (BX_M - 1), k8 = e >> 7;
+                const int b0 = k0 + k8 * 8;
+                const uint32_t bits = (umask[m * W + (b0 >> 5)] >> (b0 & 31)) & 0xffu;
+                const uint32_t bad = (bw[(k8 * 8) >> 5] >> ((k8 * 8) & 31)) & 0xffu;
+                if (bits & bad) pdefer[m] = 1;
+                uint32_t v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    v[q] = ((bits >> (2 * q)) & 1u ? 0x3F80u : 0u) | ((bits >> (2 * q + 1)) & 1u ? 0x3F800000u : 0u);
+                *reinterpret_cast<uint4 *>(As + (m >> 3) * L::SBO + k8 * 128 + (m & 7) * 16) =
+                    make_uint4(v[0], v[1], v[2], v[3]);
+            }
+            // ---- B: outer-product entries, hi and lo ----
+            for (int e = tid; e < 32 * (KC / 8); e += BX_THREADS) {
+                const int bl = e & 31, k8 = e >> 5;
+                if (bl * 8 >= nmma) continue;
+                unsigned char *dh = Bh + bl * L::SBO + k8 * 128;
+                unsigned char *dl = Bl + bl * L::SBO + k8 * 128;
+                if (bl * 8 >= ncol) {
+                    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        *reinterpret_cast<uint4 *>(dh + c * 16) = z;
+                        *reinterpret_cast<uint4 *>(dl + c * 16) = z;
+                    }
+                    continue;
+                }
+                const short2 ab = blk[cb / 8 + bl];
+                const unsigned char *xa = Xb + ab.x * L::XRS + k8 * 128;
+                const unsigned char *xb = Xb + ab.y * L::XRS + k8 * 128;
+                float4 pa[8], pb[8];   // per sample: x_{2a}, x_{2a+1} / x_{2b}, x_{2b+1}
+#pragma unroll
+                for (int q = 0; q < 8; ++q) pa[q] = *reinterpret_cast<const float4 *>(xa + q * 16);
+                if (ab.x != ab.y) {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) pb[q] = *reinterpret_cast<const float4 *>(xb + q * 16);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) pb[q] = pa[q];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int ia = u >> 1, jb = u & 1;     // i = 2a + ia, j = 2b + jb
+                    float re[8], im[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float xr = ia ? pa[q].z : pa[q].x, xi = ia ? pa[q].w : pa[q].y;
+                        const float yr = jb ? pb[q].z : pb[q].x, yi = jb ? pb[q].w : pb[q].y;
+                        re[q] = fmaf(xr, yr, xi * yi);          // Re x_i conj(x_j)
+                        im[q] = fmaf(xi, yr, -(xr * yi));       // Im x_i conj(x_j)
+                    }
+                    store_split(dh + (2 * u) * 16, dl + (2 * u) * 16, re);
+                    store_split(dh + (2 * u + 1) * 16, dl + (2 * u + 1) * 16, im);
+                }
+            }
+            fence_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                fence_after_sync();
+                const uint32_t a0 = smem_addr(As), h0 = smem_addr(Bh), l0 = smem_addr(Bl);
+#pragma unroll
+                for (int kk = 0; kk < KC / 16; ++kk) {
+                    const uint64_t da = make_smem_desc(a0 + kk * 256, 128, L::SBO);
+                    const uint64_t dh = make_smem_desc(h0 + kk * 256, 128, L::SBO);
+                    const uint64_t dl = make_smem_desc(l0 + kk * 256, 128, L::SBO);
+                    tc_mma(tbase, da, dh, idesc, (ch > 0 || kk > 0) ? 1u : 0u);
+                    tc_mma(tbase, da, dl, idesc, 1u);
+                }
+                tc_commit(&mbar[s]);
+            }
+            st.pend |= 1u << s;
+            ++st.gstep;
+            // every thread has finished building this chunk (barrier
+            // above): the prefetched samples replace it in Xb; the next
+            // iteration's wait is the barrier before they are read
+            if (more) put(badw + (s ^ 1) * (KC / 32));
+        }
+        if (st.timed_out) return;
+        if (!box_wait(mbar, st, 0) || !box_wait(mbar, st, 1)) { st.timed_out = true; break; }
+        fence_after_sync();
+        // ---- epilogue: warp w reads TMEM lanes 32(w%4).., 128 columns ----
+        {
+            const int q = warp & 3, h = warp >> 2;
+            const int m = 32 * q + lane;
+            const bool store = pinfo[m] >= 0 && !pdefer[m];
+            const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
+            float *dst = reinterpret_cast<float *>(P.cbuf) + (store ? loc * P.cstride + cb : 0ll);
+            for (int c32 = 4 * h; c32 < 4 * h + 4; ++c32) {
+                const int col0 = 32 * c32;
+                if (col0 >= ncol) break;
+                uint32_t v[32];
+                tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)col0, v);
+                tmem_wait_ld();
+                if (store) {
+                    const int lim = min(32, ncol - col0);
+#pragma unroll
+                    for (int j = 0; j < 32; j += 4)
+                        if (j < lim)
+                            *reinterpret_cast<float4 *>(dst + col0 + j) =
+                                make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
+                                            __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
+                }
+            }
+        }
+        fence_before_sync();
+        __syncthreads();
+    }
+    if (st.timed_out) return;
+    if (tid < BX_M) {
+        const int m = tid, info = pinfo[m];
+        if (info != CI_SKIP) {
+            const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
+            P.cinfo[loc] = (info >= 0 && pdefer[m]) ? CI_DEFER : info;
+        }
+    }
+    __syncthreads();
+
+}
+
+template <int KC>
+__device__ __forceinline__ uint32_t box_setup(unsigned char *smem, BoxPipe &st)
+{
+    using L = BoxLay<KC>;
+    unsigned char *misc = smem + L::OFF_MISC;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(misc + 16);
+    uint32_t *badw = reinterpret_cast<uint32_t *>(misc + 32);
+    const int tid = threadIdx.x, warp = tid >> 5;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                      :: "r"(smem_addr(tmem_slot)), "r"(BX_NCOL) : "memory");
@@ -219,270 +502,32 @@ __global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
         mbar_init(&mbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    for (int b = tid; b < nblk; b += BX_THREADS) {
-        int a = 0, rem = b;
-        while (rem >= dp - a) { rem -= dp - a; ++a; }
-        blk[b] = make_short2((short)a, (short)(a + rem));
-    }
     if (tid < 2 * (KC / 32)) badw[tid] = 0;
+    st.pend = 0;
+    st.par = 0;
+    st.gstep = 0;
+    st.timed_out = false;
+    st.blk_dp = -1;
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
-    const uint32_t tbase = *tmem_slot;
+    return *tmem_slot;
+}
 
-    uint32_t pend = 0, par = 0;     // per stage: MMAs in flight, barrier parity
-    unsigned gstep = 0;
-    bool timed_out = false;
-    // wait until the MMAs reading stage s are complete; the vote keeps the
-    // timeout decision uniform across the CTA
-    auto wait_stage = [&](int s) -> bool {
-        bool late = false;
-        if (pend & (1u << s)) {
-            long long spins = 0;
-            while (!mbar_try_wait(&mbar[s], (par >> s) & 1u)) {
-                if (++spins > BX_SPIN_LIMIT) { late = true; break; }
-            }
-            if (!late) { par ^= 1u << s; pend &= ~(1u << s); }
-        }
-        return __syncthreads_or(late) == 0;
-    };
-
-    for (long long t = blockIdx.x; t < ntiles && !timed_out; t += gridDim.x) {
-        const int R0 = ra + int(t / ntc) * BX_TR, C0 = int(t % ntc) * BX_TC;
-        // ---- per-pixel SHP masks over the union samples ----------------
-        for (int e = tid; e < BX_M * W; e += BX_THREADS) umask[e] = 0;
-        for (int e = tid; e < BX_M * nul; e += BX_THREADS) {
-            const int m = e / nul, w = e - m * nul;
-            const int r = R0 + m / BX_TC, c = C0 + m % BX_TC;
-            nm[e] = (r < rb && c < cols) ? __ldg(P.nmap + ((long long)r * cols + c) * nul + w) : 0u;
-        }
-        __syncthreads();
-        for (int e = tid; e < BX_M * wy; e += BX_THREADS) {
-            const int m = e / wy, a = e - m * wy;
-            const int tr = m / BX_TC, tc = m % BX_TC;
-            const int r = R0 + tr, c = C0 + tc;
-            const int sr = r - P.ny + a;                    // image row of window row a
-            if (r >= rb || c >= cols || sr < 0 || sr >= rows) continue;
-            uint64_t bits = extract_bits(nm + m * nul, nul, a * wx, wx);
-            // window column b is image column c - nx + b (evd.cpp:530-534)
-            const int blo = max(0, P.nx - c), bhi = min(wx, cols - c + P.nx);
-            if (bhi <= blo) continue;
-            bits &= ((1ull << (bhi - blo)) - 1ull) << blo;
-            if (!bits) continue;
-            const int pos = (tr + a) * uwp + tc;            // union sample of window (a, 0)
-            const int w0 = pos >> 5, sh = pos & 31;
-            const uint64_t lo = bits << sh;
-            const uint32_t hi = sh ? (uint32_t)(bits >> (64 - sh)) : 0u;
-            uint32_t *um = umask + m * W;
-            if ((uint32_t)lo) atomicOr(um + w0, (uint32_t)lo);
-            if ((uint32_t)(lo >> 32)) atomicOr(um + w0 + 1, (uint32_t)(lo >> 32));
-            if (hi) atomicOr(um + w0 + 2, hi);
-        }
-        __syncthreads();
-        if (tid < BX_M) {
-            const int m = tid, r = R0 + m / BX_TC, c = C0 + m % BX_TC;
-            int info = CI_SKIP;
-            if (r < rb && c < cols) {
-                const int cflat = P.ny * wx + P.nx;
-                if (!((nm[m * nul + (cflat >> 5)] >> (cflat & 31)) & 1u)) {
-                    info = CI_CENTRE;                       // evd.cpp:517
-                } else {
-                    int cnt = 0;
-                    for (int w = 0; w < W; ++w) cnt += __popc(umask[m * W + w]);
-                    info = (cnt < min_neigh) ? CI_FEW : cnt;
-                }
-            }
-            pinfo[m] = info;
-            pdefer[m] = 0;
-        }
-        // (the first chunk's barriers order these before any use)
-
-        // samples of chunk k0 (date pairs interleaved): each thread loads one
-        // sample for up to BX_XPT dates into registers; put() stores them in
-        // Xb and flags samples outside the split range for the stage's mask
-        constexpr int BX_XPT = 8;
-        const int sidx = tid % KC, d0 = tid / KC;
-        float2 xv[BX_XPT];
-        bool xbad = false;
-        auto fetch = [&](int k0) {
-            const int k = k0 + sidx;
-            const int ur = k / uwp, uc = k - ur * uwp;
-            const int r = R0 - P.ny + ur, c = C0 - P.nx + uc;
-            const bool valid = uc < uw && ur < uh && r >= 0 && r < rows && c >= 0 && c < cols;
-            const float2 *src = P.stack + (valid ? (long long)r * cols + c : 0ll);
-            xbad = false;
-#pragma unroll
-            for (int q = 0; q < BX_XPT; ++q) {
-                const int d = d0 + q * (BX_THREADS / KC);
-                float2 x = make_float2(0.f, 0.f);
-                if (valid && d < n) x = __ldg(src + d * plane);
-                xv[q] = x;
-            }
-        };
-        auto put = [&](uint32_t *bw) {
-#pragma unroll
-            for (int q = 0; q < BX_XPT; ++q) {
-                const int d = d0 + q * (BX_THREADS / KC);
-                if (d >= 2 * dp) break;
-                float2 x = xv[q];
-                if (!split_range(x.x) || !split_range(x.y)) {
-                    xbad = true;
-                    x = make_float2(0.f, 0.f);
-                }
-                *reinterpret_cast<float2 *>(Xb + (d >> 1) * L::XRS + sidx * 16 + (d & 1) * 8) = x;
-            }
-            if (xbad) atomicOr(bw + (sidx >> 5), 1u << (sidx & 31));
-        };
-        // prologue: the first chunk of the tile into Xb (its stage's flags
-        // were cleared when that stage was last used, or at start-up)
-        fetch(0);
-        put(badw + (gstep & 1) * (KC / 32));
-        __syncthreads();
-
-        for (int pass = 0; pass < npass && !timed_out; ++pass) {
-            const int cb = pass * BX_NCOL;
-            const int ncol = min(BX_NCOL, ncolt - cb);
-            const int nmma = (ncol + 15) & ~15;
-            const uint32_t idesc = make_idesc(nmma);
-            for (int ch = 0; ch < nchunk; ++ch) {
-                const int s = gstep & 1;
-                if (!wait_stage(s)) { timed_out = true; break; }
-                unsigned char *As = smem + s * L::STAGE;
-                unsigned char *Bh = As + L::A_BYTES, *Bl = Bh + L::B_BYTES;
-                uint32_t *bw = badw + s * (KC / 32);
-                const int k0 = ch * KC;
-                // the next chunk (the first chunk again after the last one of
-                // a pass) is loaded while this one is built
-                const bool more = (ch + 1 < nchunk) || (pass + 1 < npass);
-                if (more) fetch(ch + 1 < nchunk ? k0 + KC : 0);
-                if (tid < KC / 32) badw[(s ^ 1) * (KC / 32) + tid] = 0;   // for the next chunk
-                // ---- A: SHP mask rows ----
-                for (int e = tid; e < BX_M * (KC / 8); e += BX_THREADS) {
-                    const int m = e & (BX_M - 1), k8 = e >> 7;
-                    const int b0 = k0 + k8 * 8;
-                    const uint32_t bits = (umask[m * W + (b0 >> 5)] >> (b0 & 31)) & 0xffu;
-                    const uint32_t bad = (bw[(k8 * 8) >> 5] >> ((k8 * 8) & 31)) & 0xffu;
-                    if (bits & bad) pdefer[m] = 1;
-                    uint32_t v[4];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        v[q] = ((bits >> (2 * q)) & 1u ? 0x3F80u : 0u) | ((bits >> (2 * q + 1)) & 1u ? 0x3F800000u : 0u);
-                    *reinterpret_cast<uint4 *>(As + (m >> 3) * L::SBO + k8 * 128 + (m & 7) * 16) =
-                        make_uint4(v[0], v[1], v[2], v[3]);
-                }
-                // ---- B: outer-product entries, hi and lo ----
-                for (int e = tid; e < 32 * (KC / 8); e += BX_THREADS) {
-                    const int bl = e & 31, k8 = e >> 5;
-                    if (bl * 8 >= nmma) continue;
-                    unsigned char *dh = Bh + bl * L::SBO + k8 * 128;
-                    unsigned char *dl = Bl + bl * L::SBO + k8 * 128;
-                    if (bl * 8 >= ncol) {
-                        const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-                        for (int c = 0; c < 8; ++c) {
-                            *reinterpret_cast<uint4 *>(dh + c * 16) = z;
-                            *reinterpret_cast<uint4 *>(dl + c * 16) = z;
-                        }
-                        continue;
-                    }
-                    const short2 ab = blk[cb / 8 + bl];
-                    const unsigned char *xa = Xb + ab.x * L::XRS + k8 * 128;
-                    const unsigned char *xb = Xb + ab.y * L::XRS + k8 * 128;
-                    float4 pa[8], pb[8];   // per sample: x_{2a}, x_{2a+1} / x_{2b}, x_{2b+1}
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) pa[q] = *reinterpret_cast<const float4 *>(xa + q * 16);
-                    if (ab.x != ab.y) {
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) pb[q] = *reinterpret_cast<const float4 *>(xb + q * 16);
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) pb[q] = pa[q];
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int ia = u >> 1, jb = u & 1;     // i = 2a + ia, j = 2b + jb
-                        float re[8], im[8];
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) {
-                            const float xr = ia ? pa[q].z : pa[q].x, xi = ia ? pa[q].w : pa[q].y;
-                            const float yr = jb ? pb[q].z : pb[q].x, yi = jb ? pb[q].w : pb[q].y;
-                            re[q] = fmaf(xr, yr, xi * yi);          // Re x_i conj(x_j)
-                            im[q] = fmaf(xi, yr, -(xr * yi));       // Im x_i conj(x_j)
-                        }
-                        store_split(dh + (2 * u) * 16, dl + (2 * u) * 16, re);
-                        store_split(dh + (2 * u + 1) * 16, dl + (2 * u + 1) * 16, im);
-                    }
-                }
-                fence_async_smem();
-                __syncthreads();
-                if (tid == 0) {
-                    fence_after_sync();
-                    const uint32_t a0 = smem_addr(As), h0 = smem_addr(Bh), l0 = smem_addr(Bl);
-#pragma unroll
-                    for (int kk = 0; kk < KC / 16; ++kk) {
-                        const uint64_t da = make_smem_desc(a0 + kk * 256, 128, L::SBO);
-                        const uint64_t dh = make_smem_desc(h0 + kk * 256, 128, L::SBO);
-                        const uint64_t dl = make_smem_desc(l0 + kk * 256, 128, L::SBO);
-                        tc_mma(tbase, da, dh, idesc, (ch > 0 || kk > 0) ? 1u : 0u);
-                        tc_mma(tbase, da, dl, idesc, 1u);
-                    }
-                    tc_commit(&mbar[s]);
-                }
-                pend |= 1u << s;
-                ++gstep;
-                // every thread has finished building this chunk (barrier
-                // above): the prefetched samples replace it in Xb; the next
-                // iteration's wait is the barrier before they are read
-                if (more) put(badw + (s ^ 1) * (KC / 32));
-            }
-            if (timed_out) break;
-            if (!wait_stage(0) || !wait_stage(1)) { timed_out = true; break; }
-            fence_after_sync();
-            // ---- epilogue: warp w reads TMEM lanes 32(w%4).., 128 columns ----
-            {
-                const int q = warp & 3, h = warp >> 2;
-                const int m = 32 * q + lane;
-                const bool store = pinfo[m] >= 0 && !pdefer[m];
-                const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
-                float *dst = reinterpret_cast<float *>(P.cbuf) + (store ? loc * P.cstride + cb : 0ll);
-                for (int c32 = 4 * h; c32 < 4 * h + 4; ++c32) {
-                    const int col0 = 32 * c32;
-                    if (col0 >= ncol) break;
-                    uint32_t v[32];
-                    tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)col0, v);
-                    tmem_wait_ld();
-                    if (store) {
-                        const int lim = min(32, ncol - col0);
-#pragma unroll
-                        for (int j = 0; j < 32; j += 4)
-                            if (j < lim)
-                                *reinterpret_cast<float4 *>(dst + col0 + j) =
-                                    make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
-                                                __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
-                    }
-                }
-            }
-            fence_before_sync();
-            __syncthreads();
-        }
-        if (timed_out) break;
-        if (tid < BX_M) {
-            const int m = tid, info = pinfo[m];
-            if (info != CI_SKIP) {
-                const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
-                P.cinfo[loc] = (info >= 0 && pdefer[m]) ? CI_DEFER : info;
-            }
-        }
-        __syncthreads();
-    }
-    if (timed_out) {
-        if (tid == 0) atomicOr(P.err, ERR_TC_TIMEOUT);
-        // give the MMAs in flight a second bounded wait before their tensor
-        // memory is released
+// on a timeout: record the error, give the MMAs in flight a second bounded
+// wait; then release the tensor memory
+template <int KC>
+__device__ __forceinline__ void box_teardown(unsigned char *smem, uint32_t tbase, BoxPipe &st, unsigned *err)
+{
+    using L = BoxLay<KC>;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + L::OFF_MISC);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (st.timed_out) {
+        if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
         for (int s = 0; s < 2; ++s) {
-            if (pend & (1u << s)) {
+            if (st.pend & (1u << s)) {
                 long long spins = 0;
-                while (!mbar_try_wait(&mbar[s], (par >> s) & 1u) && ++spins < BX_SPIN_LIMIT) {
+                while (!mbar_try_wait(&mbar[s], (st.par >> s) & 1u) && ++spins < BX_SPIN_LIMIT) {
                 }
             }
         }
@@ -496,26 +541,88 @@ __global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
 }
 
 template <int KC>
+__global__ void __launch_bounds__(BX_THREADS, 1) k_gram_box(KParams P)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    BoxPipe st;
+    const uint32_t tbase = box_setup<KC>(smem, st);
+    const long long ntiles = box_tiles(P);
+    for (long long t = blockIdx.x; t < ntiles && !st.timed_out; t += gridDim.x)
+        box_tile<KC>(P, t, smem, tbase, st);
+    box_teardown<KC>(smem, tbase, st, P.err);
+}
+
+// Many launches' tiles in one persistent launch: segment s covers tiles
+// [segs[s].tile_offset, segs[s+1].tile_offset) of the concatenation.
+template <int KC>
+__global__ void __launch_bounds__(BX_THREADS, 1) k_gram_batch(const BoxSeg *__restrict__ segs, int nseg,
+                                                              long long total)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    BoxPipe st;
+    const uint32_t tbase = box_setup<KC>(smem, st);
+    for (long long t = blockIdx.x; t < total && !st.timed_out; t += gridDim.x) {
+        int lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (segs[mid].tile_offset <= t) lo = mid; else hi = mid - 1;
+        }
+        box_tile<KC>(segs[lo].P, t - segs[lo].tile_offset, smem, tbase, st);
+    }
+    box_teardown<KC>(smem, tbase, st, segs[0].P.err);
+}
+
+template <int KC>
+size_t box_smem(int ny, int nx)
+{
+    using L = BoxLay<KC>;
+    const int uh = BX_TR + 2 * ny, uwp = (BX_TC + 2 * nx + 7) & ~7;
+    const int kp = (uh * uwp + KC - 1) / KC * KC;
+    return L::OFF_U + (size_t)BX_M * (kp / 32) * 4;
+}
+
+// per-kernel flags: attributes set once per device
+template <int KC, bool BATCH>
+bool *box_flags()
+{
+    static bool f[64] = {false};
+    return f;
+}
+
+template <typename K>
+cudaError_t box_configure(K kern, size_t smem_max, bool *configured)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && configured[dev]) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    if (e == cudaSuccess && dev < 64) configured[dev] = true;
+    return e;
+}
+
+template <int KC>
 cudaError_t launch_box_t(const KParams &P, int num_sms, cudaStream_t st)
 {
     using L = BoxLay<KC>;
-    static bool configured[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 64 && !configured[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_gram_box<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)L::MAX_SMEM);
-        if (e != cudaSuccess) return e;
-        configured[dev] = true;
-    }
-    const int uh = BX_TR + 2 * P.ny, uwp = (BX_TC + P.wx - 1 + 7) & ~7;
-    const int kp = (uh * uwp + KC - 1) / KC * KC;
-    const size_t smem = L::OFF_U + (size_t)BX_M * (kp / 32) * 4;
-    const long long nrows = P.npix / P.cols;
-    const long long ntiles = ((P.cols + BX_TC - 1) / BX_TC) * ((nrows + BX_TR - 1) / BX_TR);
+    cudaError_t e = box_configure(k_gram_box<KC>, L::MAX_SMEM, box_flags<KC, false>());
+    if (e != cudaSuccess) return e;
+    const long long ntiles = box_tiles(P);
     long long blocks = num_sms;
     if (ntiles < blocks) blocks = ntiles > 0 ? ntiles : 1;
-    k_gram_box<KC><<<(unsigned)blocks, BX_THREADS, smem, st>>>(P);
+    k_gram_box<KC><<<(unsigned)blocks, BX_THREADS, box_smem<KC>(P.ny, P.nx), st>>>(P);
+    return cudaGetLastError();
+}
+
+template <int KC>
+cudaError_t launch_box_batch_t(const BoxSeg *segs, int nseg, long long total, size_t smem, int num_sms,
+                               cudaStream_t st)
+{
+    using L = BoxLay<KC>;
+    cudaError_t e = box_configure(k_gram_batch<KC>, L::MAX_SMEM, box_flags<KC, true>());
+    if (e != cudaSuccess) return e;
+    long long blocks = num_sms;
+    if (total < blocks) blocks = total > 0 ? total : 1;
+    k_gram_batch<KC><<<(unsigned)blocks, BX_THREADS, smem, st>>>(segs, nseg, total);
     return cudaGetLastError();
 }
 
@@ -533,6 +640,31 @@ int gram_box_record(int nb)
 {
     const int dp = (nb + 1) >> 1;
     return 8 * (dp * (dp + 1) / 2);
+}
+
+int gram_box_kc(int nb) { return nb <= 32 ? 64 : 32; }
+
+long long gram_box_tiles(const KParams &P) { return box_tiles(P); }
+
+size_t gram_box_smem(int nb, int ny, int nx)
+{
+    return gram_box_kc(nb) == 64 ? box_smem<64>(ny, nx) : box_smem<32>(ny, nx);
+}
+
+cudaError_t prepare_gram_batch()
+{
+    cudaError_t e = box_configure(k_gram_batch<64>, BoxLay<64>::MAX_SMEM, box_flags<64, true>());
+    if (e == cudaSuccess) e = box_configure(k_gram_batch<32>, BoxLay<32>::MAX_SMEM, box_flags<32, true>());
+    return e;
+}
+
+cudaError_t launch_gram_batch(int kc, const BoxSeg *segs, int nseg, long long total, size_t smem, int num_sms,
+                              cudaStream_t st)
+{
+    if (nseg <= 0 || total <= 0) return cudaSuccess;
+    if (kc == 64) return launch_box_batch_t<64>(segs, nseg, total, smem, num_sms, st);
+    if (kc == 32) return launch_box_batch_t<32>(segs, nseg, total, smem, num_sms, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_gram_box(const KParams &P, int num_sms, cudaStream_t st)

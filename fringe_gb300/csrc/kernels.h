@@ -7,6 +7,8 @@
 namespace fpl {
 
 struct KParams;
+struct BoxSeg;
+struct BatchEntry;
 
 // padded order used for a stack depth (16, 32, 64; 0 = unsupported)
 int pick_np(int nb);
@@ -31,5 +33,23 @@ cudaError_t launch_gram_box(const KParams &P, int num_sms, cudaStream_t st);
 
 // mixed form: eigen-solves and outputs from P.cbuf / P.cinfo
 cudaError_t launch_solve(const KParams &P, int num_sms, cudaStream_t st);
+
+// batched mixed form.  Launches of one Gamma kernel share its sample-chunk
+// width (gram_box_kc: 64 for <= 32 dates, 32 above); one launch covers
+// gram_box_tiles(P) tiles and needs gram_box_smem bytes of shared memory.
+int gram_box_kc(int nb);
+long long gram_box_tiles(const KParams &P);
+size_t gram_box_smem(int nb, int ny, int nx);
+// tiles of every segment in one persistent launch (smem: the largest
+// gram_box_smem of the segments)
+cudaError_t launch_gram_batch(int kc, const BoxSeg *segs, int nseg, long long total, size_t smem,
+                              int num_sms, cudaStream_t st);
+// kernel attributes of the batched mixed form for padded depth np (call
+// before capturing a launch sequence)
+cudaError_t prepare_mixed_batch(int np);
+cudaError_t prepare_gram_batch();
+// eigen-solves of every entry (one padded depth np) in one persistent launch
+cudaError_t launch_solve_batch(int np, const BatchEntry *ents, int nent, long long total, int num_sms,
+                               cudaStream_t st);
 
 }  // namespace fpl

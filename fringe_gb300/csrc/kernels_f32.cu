@@ -31,4 +31,28 @@ cudaError_t launch_solve(const KParams &P, int num_sms, cudaStream_t st)
     return cudaErrorInvalidValue;
 }
 
+cudaError_t prepare_mixed_batch(int np)
+{
+    cudaError_t e = prepare_gram_batch();
+    if (e != cudaSuccess) return e;
+    switch (np) {
+    case 16: return configure_solve_batch<16, true>();
+    case 32: return configure_solve_batch<32, true>();
+    case 64: return configure_solve_batch<64, false>();
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_solve_batch(int np, const BatchEntry *ents, int nent, long long total, int num_sms,
+                               cudaStream_t st)
+{
+    if (nent <= 0 || total <= 0) return cudaSuccess;
+    switch (np) {
+    case 16: return launch_solve_batch_t<16, true>(ents, nent, total, num_sms, st);
+    case 32: return launch_solve_batch_t<32, true>(ents, nent, total, num_sms, st);
+    case 64: return launch_solve_batch_t<64, false>(ents, nent, total, num_sms, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
 }  // namespace fpl

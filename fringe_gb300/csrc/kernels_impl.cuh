@@ -43,8 +43,27 @@ __device__ __forceinline__ int tmem_cols_for(int warps, int np)
     return cols;
 }
 
-template <int NP, bool TM>
-__global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve(KParams P)
+// pixel pp of the launch P: record -> coherence rows -> solve and outputs
+template <int NP, typename CP>
+__device__ __forceinline__ void solve_pixel(const KParams &P, long long pp, unsigned char *sm, int lane, const CP &cp,
+                                            C2<float> *A)
+{
+    if constexpr (NP <= 32) {
+        const int npix = pixel_load_gamma<NP, false>(P, pp, sm, lane, A);
+        if (npix >= 0 && rows_coherence<NP>(P, pp, A, sm, cp, lane))
+            pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
+    } else {
+        const int npix = pixel_load_gamma<NP>(P, pp, sm, lane, A);
+        if (npix >= 0) pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
+    }
+}
+
+// Solve kernel over a pixel source: SRC(q) gives (launch, pixel) of item q
+// of [0, total).  TM: each warp keeps its pixel's coherence rows in tensor
+// memory (2*NP columns of its 32-lane quadrant) instead of shared memory,
+// so a CTA holds about twice as many warps; the kernel issues no MMA.
+template <int NP, bool TM, typename SRC>
+__device__ __forceinline__ void solve_loop(long long total, const SRC &src)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warps = blockDim.x >> 5;
@@ -67,11 +86,10 @@ __global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve(KParams P)
         const uint32_t tbase = tslot;
         const CRowsTmem<NP> cp{tbase + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * 2 * NP)};
         C2<float> *A = reinterpret_cast<C2<float> *>(sm + Lay<float, NP>::wm);
-        for (long long q = gw; q < P.npix; q += nw) {
-            const long long pp = P.pix_begin + q;
-            const int npix = pixel_load_gamma<NP, false>(P, pp, sm, lane, A);
-            if (npix >= 0 && rows_coherence<NP>(P, pp, A, sm, cp, lane))
-                pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
+        for (long long q = gw; q < total; q += nw) {
+            long long pp;
+            const KParams &P = src(q, pp);
+            solve_pixel<NP>(P, pp, sm, lane, cp, A);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
@@ -82,35 +100,50 @@ __global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve(KParams P)
     } else {
         C2<float> *Cm = reinterpret_cast<C2<float> *>(sm + Lay<float, NP>::cm);
         const CRowsSmem<float, NP> cp{Cm, lane};
-        for (long long q = gw; q < P.npix; q += nw) {
-            const long long pp = P.pix_begin + q;
-            const int npix = pixel_load_gamma<NP>(P, pp, sm, lane, Cm);
-            if (npix >= 0) pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
+        for (long long q = gw; q < total; q += nw) {
+            long long pp;
+            const KParams &P = src(q, pp);
+            solve_pixel<NP>(P, pp, sm, lane, cp, Cm);
         }
     }
 }
 
 template <int NP, bool TM>
-static cudaError_t launch_solve_t(const KParams &P, int num_sms, cudaStream_t st)
+__global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve(KParams P)
 {
-    static bool configured[64] = {false};
+    solve_loop<NP, TM>(P.npix, [&](long long q, long long &pp) -> const KParams & {
+        pp = P.pix_begin + q;
+        return P;
+    });
+}
+
+// the mixed form over many launches of one padded depth
+template <int NP, bool TM>
+__global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve_batch(const BatchEntry *__restrict__ ents, int nent,
+                                                                  long long total)
+{
+    solve_loop<NP, TM>(total, [&](long long q, long long &pp) -> const KParams & {
+        int lo = 0, hi = nent - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (ents[mid].px_offset <= q) lo = mid; else hi = mid - 1;
+        }
+        pp = ents[lo].P.pix_begin + (q - ents[lo].px_offset);
+        return ents[lo].P;
+    });
+}
+
+// CTA shape of the solve kernels: warps per CTA by shared memory (and
+// registers), one CTA per SM in the tensor-memory form
+template <int NP, bool TM, typename K>
+static cudaError_t solve_shape(K kern, int *warps_out, int *per_sm_out, size_t *smem_out)
+{
     const size_t per_warp = TM ? Lay<float, NP>::bytes_noc : Lay<float, NP>::bytes;
     const size_t budget = 224 * 1024;
     const int cap = TM ? 32 : 16;
     int warps = int(budget / per_warp);
     if (warps > cap) warps = cap;
     if (warps < 1) warps = 1;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 64 && !configured[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_solve<NP, TM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)budget);
-        if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(k_solve<NP, TM>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        if (e != cudaSuccess) return e;
-        configured[dev] = true;
-    }
-    // registers can bound the warps of a CTA below the shared-memory figure
     int per_sm = 0;
     size_t smem = per_warp * warps;
     for (;;) {
@@ -118,17 +151,70 @@ static cudaError_t launch_solve_t(const KParams &P, int num_sms, cudaStream_t st
         // one CTA per SM in the tensor-memory form: at least half the shared
         // memory, so a second CTA never waits on a tensor-memory allocation
         if (TM && smem < budget / 2 + 1024) smem = budget / 2 + 1024;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<NP, TM>, warps * 32, smem);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem);
         if (e != cudaSuccess) return e;
         if (per_sm >= 1 || warps == 1) break;
         --warps;
     }
     if (per_sm < 1) per_sm = 1;
     if (TM) per_sm = 1;
+    *warps_out = warps;
+    *per_sm_out = per_sm;
+    *smem_out = smem;
+    return cudaSuccess;
+}
+
+template <typename K>
+static cudaError_t solve_configure(K kern, bool *configured)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && configured[dev]) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 224 * 1024);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    if (dev < 64) configured[dev] = true;
+    return cudaSuccess;
+}
+
+template <int NP, bool TM>
+static cudaError_t launch_solve_t(const KParams &P, int num_sms, cudaStream_t st)
+{
+    static bool configured[64] = {false};
+    cudaError_t e = solve_configure(k_solve<NP, TM>, configured);
+    if (e != cudaSuccess) return e;
+    int warps = 0, per_sm = 0;
+    size_t smem = 0;
+    if ((e = solve_shape<NP, TM>(k_solve<NP, TM>, &warps, &per_sm, &smem)) != cudaSuccess) return e;
     long long blocks = (long long)num_sms * per_sm;
     long long need = (P.npix + warps - 1) / warps;
     if (need < blocks) blocks = need > 0 ? need : 1;
     k_solve<NP, TM><<<(unsigned)blocks, warps * 32, smem, st>>>(P);
+    return cudaGetLastError();
+}
+
+// attributes of k_solve_batch<NP, TM>, set once per device
+template <int NP, bool TM>
+static cudaError_t configure_solve_batch()
+{
+    static bool configured[64] = {false};
+    return solve_configure(k_solve_batch<NP, TM>, configured);
+}
+
+template <int NP, bool TM>
+static cudaError_t launch_solve_batch_t(const BatchEntry *ents, int nent, long long total, int num_sms,
+                                       cudaStream_t st)
+{
+    cudaError_t e = configure_solve_batch<NP, TM>();
+    if (e != cudaSuccess) return e;
+    int warps = 0, per_sm = 0;
+    size_t smem = 0;
+    if ((e = solve_shape<NP, TM>(k_solve_batch<NP, TM>, &warps, &per_sm, &smem)) != cudaSuccess) return e;
+    long long blocks = (long long)num_sms * per_sm;
+    long long need = (total + warps - 1) / warps;
+    if (need < blocks) blocks = need > 0 ? need : 1;
+    k_solve_batch<NP, TM><<<(unsigned)blocks, warps * 32, smem, st>>>(ents, nent, total);
     return cudaGetLastError();
 }
 

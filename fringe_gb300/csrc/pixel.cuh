@@ -58,6 +58,18 @@ struct KParams {
 
 enum { CI_CENTRE = -1, CI_FEW = -2, CI_DEFER = -3 };
 
+// one launch's share of a batched launch: the Gamma kernel's segment
+// (tiles [tile_offset, next segment's tile_offset)) and the solve and FP64
+// kernels' entry (pixels [px_offset, next entry's px_offset))
+struct BoxSeg {
+    KParams P;
+    long long tile_offset;
+};
+struct BatchEntry {
+    KParams P;
+    long long px_offset;   // first pixel of this entry in the class's concatenated range
+};
+
 enum { M_MLE = 0, M_EVD = 1, M_STBAS = 2 };
 enum { SEM_EVD = 0, SEM_PL = 1 };
 enum { ERR_FB_OVERFLOW = 1u };
@@ -88,6 +100,18 @@ template <typename T> __device__ __forceinline__ void cfma(C2<T> &acc, C2<T> a, 
 {
     acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
     acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+}
+
+// b -= a * y and b -= conj(a) * y as fused multiply-adds
+template <typename T> __device__ __forceinline__ void fms_mul(C2<T> &b, C2<T> a, C2<T> y)
+{
+    b.x = fma(-a.x, y.x, fma(a.y, y.y, b.x));
+    b.y = fma(-a.x, y.y, fma(-a.y, y.x, b.y));
+}
+template <typename T> __device__ __forceinline__ void fms_cmul(C2<T> &b, C2<T> a, C2<T> y)
+{
+    b.x = fma(-a.x, y.x, fma(-a.y, y.y, b.x));
+    b.y = fma(-a.x, y.y, fma(a.y, y.x, b.y));
 }
 
 template <typename T> __device__ __forceinline__ T warp_sum(T v)

@@ -9,8 +9,10 @@
 //   * runs "waves" on a compute stream: every resident job whose inputs
 //     have arrived contributes a slice of rows (a fair share of the wave's
 //     pixel budget), and the slices of all jobs run as one persistent batch
-//     launch per padded depth plus one FP64 settle launch -- jobs that arrive
-//     while a wave runs join the next wave;
+//     launch per padded depth and form (plain FP32; or, for jobs asking for
+//     the mixed-precision form, one tensor-core Gamma launch over the tiles
+//     of their slices and one solve launch) plus one FP64 settle launch --
+//     jobs that arrive while a wave runs join the next wave;
 //   * copies a finished job's outputs back on the copy stream, frees its
 //     device memory and wakes its waiters.
 // Copies overlap with waves.  Each pixel's result depends only on its own
@@ -62,6 +64,7 @@ struct Piece {
     SJob *job;
     int ra, rb;
     int np;
+    int mixed;     // 1: mixed-precision form
 };
 
 constexpr size_t kPieceCounterBytes = 64;
@@ -86,6 +89,9 @@ struct fpl_server {
     cudaEvent_t ev_wave = nullptr;
     int max_pieces = 256;
     fpl::BatchEntry *d_table = nullptr, *h_table = nullptr;
+    fpl::BoxSeg *d_segs = nullptr, *h_segs = nullptr;   // mixed pieces of a wave, by chunk width
+    void *d_rec = nullptr;                              // their Gamma records and tile infos
+    size_t rec_cap = 0;
     void *d_wave = nullptr;
     size_t wave_bytes = 0;
     int fatal = 0;
@@ -192,17 +198,43 @@ bool run_wave(fpl_server *s, std::vector<Piece> &pieces)
         const int ra = j->next_row, rb = std::min(j->r1, ra + rows);
         j->next_row = rb;
         if (!j->started) { j->started = true; j->t_first = clk::now(); }
-        pieces.push_back({j, ra, rb, fpl::pick_np(j->host.nbands)});
+        const int mixed = (j->host.precision == FPL_PREC_MIXED &&
+                           fpl::gram_box_supported(j->host.nbands, j->host.half_window_y, j->host.half_window_x))
+                              ? 1
+                              : 0;
+        pieces.push_back({j, ra, rb, fpl::pick_np(j->host.nbands), mixed});
         total += (long long)(rb - ra) * j->host.cols;
     }
-    std::stable_sort(pieces.begin(), pieces.end(), [](const Piece &a, const Piece &b) { return a.np < b.np; });
+    std::stable_sort(pieces.begin(), pieces.end(), [](const Piece &a, const Piece &b) {
+        return a.np != b.np ? a.np < b.np : a.mixed < b.mixed;
+    });
+    // Gamma records of the wave's mixed pieces
+    size_t rec_floats = 0, infos = 0;
+    for (const Piece &pc : pieces)
+        if (pc.mixed) {
+            const size_t px = (size_t)(pc.rb - pc.ra) * pc.job->host.cols;
+            rec_floats += px * fpl::gram_box_record(pc.job->host.nbands);
+            infos += px;
+        }
+    const size_t rec_bytes = (sizeof(float) * rec_floats + 255) & ~size_t(255);
+    if (rec_floats && rec_bytes + sizeof(int) * infos > s->rec_cap) {
+        // the previous wave has finished (its event was waited for)
+        if (s->d_rec) cudaFree(s->d_rec);
+        s->d_rec = nullptr;
+        s->rec_cap = 0;
+        if (cudaMalloc(&s->d_rec, rec_bytes + sizeof(int) * infos) != cudaSuccess) return false;
+        s->rec_cap = rec_bytes + sizeof(int) * infos;
+    }
+    float *recs = static_cast<float *>(s->d_rec);
+    int *rinfo = reinterpret_cast<int *>(static_cast<char *>(s->d_rec) + rec_bytes);
+    long long roff = 0, ioff = 0;
     // table (pixel offsets restart in every depth class), counters, work lists
     char *base = static_cast<char *>(s->d_wave);
     long long *lists = reinterpret_cast<long long *>(base + kPieceCounterBytes * s->max_pieces + 64);
     long long loff = 0, coff = 0;
     for (size_t e = 0; e < pieces.size(); ++e) {
         const Piece &pc = pieces[e];
-        if (e > 0 && pieces[e - 1].np != pc.np) coff = 0;
+        if (e > 0 && (pieces[e - 1].np != pc.np || pieces[e - 1].mixed != pc.mixed)) coff = 0;
         fpl::KParams &P = s->h_table[e].P;
         fpl::fill_params(P, pc.job->dev, pc.ra, pc.rb, kDefaultAmbScale, kDefaultCondMax);
         P.fb_count = reinterpret_cast<int *>(base + kPieceCounterBytes * e);
@@ -210,27 +242,66 @@ bool run_wave(fpl_server *s, std::vector<Piece> &pieces)
         P.slow = reinterpret_cast<int *>(base + kPieceCounterBytes * e + 32);
         P.fb_list = lists + loff;
         P.fb_cap = (int)P.npix;
+        if (pc.mixed) {
+            P.cbuf = reinterpret_cast<float2 *>(recs + roff);
+            P.cinfo = rinfo + ioff;
+            P.cbase = P.pix_begin;
+            P.cstride = fpl::gram_box_record(P.nb);
+            roff += P.npix * P.cstride;
+            ioff += P.npix;
+        }
         s->h_table[e].px_offset = coff;
         coff += P.npix;
         loff += P.npix;
     }
+    // Gamma segments of the mixed pieces, by chunk width (64 samples, then 32)
+    int nseg[2] = {0, 0};
+    long long tiles[2] = {0, 0};
+    size_t gsm[2] = {0, 0};
+    for (int c = 0; c < 2; ++c)
+        for (size_t e = 0; e < pieces.size(); ++e) {
+            const fpl::KParams &P = s->h_table[e].P;
+            if (!pieces[e].mixed || fpl::gram_box_kc(P.nb) != (c == 0 ? 64 : 32)) continue;
+            fpl::BoxSeg &sg = s->h_segs[nseg[0] + nseg[1]];
+            sg.P = P;
+            sg.tile_offset = tiles[c];
+            tiles[c] += fpl::gram_box_tiles(P);
+            gsm[c] = std::max(gsm[c], fpl::gram_box_smem(P.nb, P.ny, P.nx));
+            ++nseg[c];
+        }
+    if (nseg[0] + nseg[1] &&
+        cudaMemcpyAsync(s->d_segs, s->h_segs, sizeof(fpl::BoxSeg) * (nseg[0] + nseg[1]), cudaMemcpyHostToDevice,
+                        s->s_compute) != cudaSuccess)
+        return false;
     if (cudaMemcpyAsync(s->d_table, s->h_table, sizeof(fpl::BatchEntry) * pieces.size(), cudaMemcpyHostToDevice,
                         s->s_compute) != cudaSuccess)
         return false;
     if (cudaMemsetAsync(s->d_wave, 0, kPieceCounterBytes * s->max_pieces + 64, s->s_compute) != cudaSuccess)
         return false;
     unsigned long long *work = reinterpret_cast<unsigned long long *>(base + kPieceCounterBytes * s->max_pieces);
+    if (nseg[0] && fpl::launch_gram_batch(64, s->d_segs, nseg[0], tiles[0], gsm[0], s->num_sms, s->s_compute) !=
+                       cudaSuccess)
+        return false;
+    if (nseg[1] && fpl::launch_gram_batch(32, s->d_segs + nseg[0], nseg[1], tiles[1], gsm[1], s->num_sms,
+                                          s->s_compute) != cudaSuccess)
+        return false;
     size_t e = 0;
     int cls = 0;
     while (e < pieces.size()) {
-        const int np = pieces[e].np;
+        const int np = pieces[e].np, mixed = pieces[e].mixed;
         const size_t first = e;
         long long n_px = 0;
-        while (e < pieces.size() && pieces[e].np == np) n_px += s->h_table[e++].P.npix;
+        while (e < pieces.size() && pieces[e].np == np && pieces[e].mixed == mixed) n_px += s->h_table[e++].P.npix;
         if (fpl::configure_np(np) != cudaSuccess) return false;
-        if (fpl::launch_batch(np, s->d_table + first, (int)(e - first), n_px, work + cls, fpl::max_warps(np, false),
-                              s->num_sms, s->s_compute) != cudaSuccess)
+        if (mixed) {
+            if (fpl::prepare_mixed_batch(np) != cudaSuccess) return false;
+            if (fpl::launch_solve_batch(np, s->d_table + first, (int)(e - first), n_px, s->num_sms, s->s_compute) !=
+                cudaSuccess)
+                return false;
+        } else if (fpl::launch_batch(np, s->d_table + first, (int)(e - first), n_px, work + cls,
+                                     fpl::max_warps(np, false), s->num_sms, s->s_compute) != cudaSuccess) {
             return false;
+        }
         if (fpl::launch_batch64(np, s->d_table + first, (int)(e - first), s->num_sms, s->s_compute) != cudaSuccess)
             return false;
         ++cls;
@@ -358,7 +429,9 @@ int fpl_server_create(const fpl_server_config *cfg, fpl_server **out)
               cudaStreamCreateWithFlags(&s->s_compute, cudaStreamNonBlocking) == cudaSuccess &&
               cudaEventCreateWithFlags(&s->ev_wave, cudaEventDisableTiming) == cudaSuccess &&
               cudaMalloc(&s->d_table, sizeof(fpl::BatchEntry) * s->max_pieces) == cudaSuccess &&
-              cudaMallocHost(&s->h_table, sizeof(fpl::BatchEntry) * s->max_pieces) == cudaSuccess;
+              cudaMallocHost(&s->h_table, sizeof(fpl::BatchEntry) * s->max_pieces) == cudaSuccess &&
+              cudaMalloc(&s->d_segs, sizeof(fpl::BoxSeg) * s->max_pieces) == cudaSuccess &&
+              cudaMallocHost(&s->h_segs, sizeof(fpl::BoxSeg) * s->max_pieces) == cudaSuccess;
     // counters | work counters | work lists (a wave holds at most wave_pixels
     // plus one row per job beyond its share)
     s->wave_bytes = kPieceCounterBytes * s->max_pieces + 64 +
@@ -451,6 +524,9 @@ int fpl_server_destroy(fpl_server *s)
     if (s->d_wave) cudaFree(s->d_wave);
     if (s->d_table) cudaFree(s->d_table);
     if (s->h_table) cudaFreeHost(s->h_table);
+    if (s->d_segs) cudaFree(s->d_segs);
+    if (s->h_segs) cudaFreeHost(s->h_segs);
+    if (s->d_rec) cudaFree(s->d_rec);
     if (s->ev_wave) cudaEventDestroy(s->ev_wave);
     if (s->s_copy) cudaStreamDestroy(s->s_copy);
     if (s->s_compute) cudaStreamDestroy(s->s_compute);

@@ -96,11 +96,12 @@ class PhaseLinkBatch:
 
     ``jobs`` is a list of dicts with keys stack, nmap (CUDA tensors),
     half_window, and optionally method, semantics, mini_stack_count,
-    band_width, min_neighbors.  Outputs are allocated once; ``run()`` fills
+    band_width, min_neighbors, precision ("fp32" or "mixed"; default the
+    batch's ``precision``).  Outputs are allocated once; ``run()`` fills
     them (replaying a captured CUDA graph when ``graph=True``).
     """
 
-    def __init__(self, jobs, graph=True, autotune=False, device=0, ctx=None):
+    def __init__(self, jobs, graph=True, autotune=False, device=0, ctx=None, precision="fp32"):
         import torch
         self.ctx = ctx or _lib.context(device)
         self.lib = _lib.load()
@@ -119,7 +120,8 @@ class PhaseLinkBatch:
             self._keep += [stack, nmap]
             arr[k] = _make_job(nb, R, C, ny, nx, j.get("method", "MLE"), j.get("semantics", "evd"),
                                j.get("mini_stack_count", 1), j.get("band_width", -1),
-                               j.get("min_neighbors", 2), "fp32", j.get("rows"), _lib.FPL_MEM_DEVICE,
+                               j.get("min_neighbors", 2), j.get("precision", precision), j.get("rows"),
+                               _lib.FPL_MEM_DEVICE,
                                stack.data_ptr(), nmap.data_ptr(), out["phase"].data_ptr(),
                                out["tcorr"].data_ptr(), out["comp"].data_ptr(), None)
         flags = (_lib.FPL_BATCH_GRAPH if graph else 0) | (_lib.FPL_BATCH_AUTOTUNE if autotune else 0)

@@ -30,9 +30,10 @@ class Server:
         self._jobs = {}
 
     def submit(self, stack, nmap, half_window, method="MLE", semantics="evd", mini_stack_count=1,
-               band_width=-1, min_neighbors=2, out=None):
+               band_width=-1, min_neighbors=2, out=None, precision="fp32"):
         """Queue a job on host arrays; returns its ticket.  The arrays must stay
-        alive until wait() returns (the server keeps references)."""
+        alive until wait() returns (the server keeps references).  precision
+        "mixed" runs the job in the mixed-precision form."""
         stack = np.ascontiguousarray(stack, dtype=np.complex64)
         nmap = np.ascontiguousarray(nmap).view(np.uint32)
         nb, R, C = stack.shape
@@ -41,7 +42,7 @@ class Server:
                    "comp": np.zeros((R, C), np.complex64)}
         ny, nx = half_window
         job = _make_job(nb, R, C, ny, nx, method, semantics, mini_stack_count, band_width,
-                        min_neighbors, "fp32", None, _lib.FPL_MEM_HOST, stack.ctypes.data,
+                        min_neighbors, precision, None, _lib.FPL_MEM_HOST, stack.ctypes.data,
                         nmap.ctypes.data, out["phase"].ctypes.data, out["tcorr"].ctypes.data,
                         out["comp"].ctypes.data, None)
         t = ctypes.c_ulonglong()

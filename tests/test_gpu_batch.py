@@ -1,6 +1,7 @@
 """Batches: jobs of different size, stack depth, window and method in one
 persistent launch (fpl_batch_*) give exactly the results of running each
-job alone, with and without CUDA-graph replay and autotuning."""
+job alone, with and without CUDA-graph replay and autotuning, in the plain
+FP32 form, the mixed-precision form, and a mix of the two."""
 import numpy as np
 import pytest
 
@@ -27,15 +28,19 @@ def _jobs(torch):
     return jobs
 
 
-@pytest.mark.parametrize("graph,autotune", [(True, False), (False, False), (True, True)])
-def test_batch_equals_single_jobs(gpu_lib, graph, autotune):
+@pytest.mark.parametrize("graph,autotune,precision", [
+    (True, False, "fp32"), (False, False, "fp32"), (True, True, "fp32"),
+    (True, False, "mixed"), (False, False, "mixed"), (True, False, "both")])
+def test_batch_equals_single_jobs(gpu_lib, graph, autotune, precision):
     torch = pytest.importorskip("torch")
     from fringe_gb300.linker import PhaseLinkBatch, phase_link
     jobs = _jobs(torch)
+    for k, j in enumerate(jobs):
+        j["precision"] = precision if precision != "both" else ("mixed" if k % 2 else "fp32")
     ref = []
     for j in jobs:
         r = phase_link(j["stack"], j["nmap"], j["half_window"], method=j["method"],
-                       mini_stack_count=j["mini_stack_count"])
+                       mini_stack_count=j["mini_stack_count"], precision=j["precision"])
         ref.append({k: v.clone() for k, v in r.items()})
     torch.cuda.synchronize()
     b = PhaseLinkBatch(jobs, graph=graph, autotune=autotune)
@@ -51,4 +56,26 @@ def test_batch_equals_single_jobs(gpu_lib, graph, autotune):
                 assert np.array_equal(a, c, equal_nan=True), (k, key, rep)
     st = b.stats()
     assert st["pixels"] == sum(R * C for R, C, *_ in SPECS)
+    b.close()
+
+
+def test_mixed_batch_over_several_waves(gpu_lib):
+    """Mixed-form jobs larger than one wave (2^20 pixels) are cut into row
+    pieces whose tiles straddle piece boundaries; results still equal the
+    single runs bit for bit."""
+    torch = pytest.importorskip("torch")
+    from fringe_gb300.linker import PhaseLinkBatch, phase_link
+    jobs = []
+    for R, C, N, ny, nx, seed in [(1100, 1000, 12, 3, 5, 31), (300, 700, 30, 5, 10, 32)]:
+        st, nm = synth.scene("voronoi", R, C, N, ny, nx, seed=seed)
+        jobs.append({"stack": torch.from_numpy(st).cuda(), "nmap": torch.from_numpy(nm.view(np.int32)).cuda(),
+                     "half_window": (ny, nx), "method": "MLE", "precision": "mixed"})
+    ref = [{k: v.clone() for k, v in phase_link(j["stack"], j["nmap"], j["half_window"],
+                                                 precision="mixed").items()} for j in jobs]
+    b = PhaseLinkBatch(jobs, graph=True)
+    out = b.run()
+    torch.cuda.synchronize()
+    for o, r in zip(out, ref):
+        for key in ("phase", "tcorr", "comp"):
+            assert np.array_equal(o[key].cpu().numpy(), r[key].cpu().numpy(), equal_nan=True), key
     b.close()

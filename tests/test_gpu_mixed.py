@@ -110,3 +110,17 @@ def test_mixed_out_of_range_samples(gpu_lib):
         assert_parity(m, phase_tol=1e-3, tcorr_tol=2e-4)
         # the NaN neighbourhood reports the oracle's codes
         assert np.array_equal(g["tcorr"][3:8, 4:11] < 0, o["tcorr"][3:8, 4:11] < 0)
+
+
+def test_mixed_results_do_not_depend_on_row_ranges(gpu_lib):
+    """Tiles sit on the absolute 8-row grid, so a pixel's coherence matrix is
+    accumulated in the same order whatever row range a run covers: the scene
+    run in pieces that do not start on the grid equals the whole run."""
+    from fringe_gb300 import phase_link
+    stack, nmap = synth.scene("voronoi", 45, 52, 20, 5, 10, seed=44)
+    whole = phase_link(stack, nmap, (5, 10), precision="mixed")
+    parts = None
+    for r0, r1 in ((0, 13), (13, 30), (30, 45)):
+        parts = phase_link(stack, nmap, (5, 10), precision="mixed", rows=(r0, r1), out=parts)
+    for key in ("phase", "tcorr", "comp"):
+        assert np.array_equal(whole[key], parts[key], equal_nan=True), key

@@ -18,16 +18,20 @@ SPECS = [  # (rows, cols, nbands, ny, nx, method, seed)
 ]
 
 
-@pytest.mark.parametrize("budget_mb", [4096, 6])
-def test_served_results_equal_single_runs(gpu_lib, budget_mb):
+@pytest.mark.parametrize("budget_mb,precision", [(4096, "fp32"), (6, "fp32"), (4096, "mixed"), (6, "both")])
+def test_served_results_equal_single_runs(gpu_lib, budget_mb, precision):
     from fringe_gb300 import phase_link
     from fringe_gb300.serve import Server
     scenes = [synth.scene("voronoi", R, C, N, ny, nx, seed=sd) for R, C, N, ny, nx, m, sd in SPECS]
-    ref = [phase_link(st, nm, (ny, nx), method=m) for (st, nm), (R, C, N, ny, nx, m, sd) in zip(scenes, SPECS)]
-    # a small wave budget forces several waves per job; a small memory budget
-    # forces admission to wait for earlier jobs to finish
+    precs = [precision if precision != "both" else ("mixed" if k % 2 else "fp32") for k in range(len(SPECS))]
+    ref = [phase_link(st, nm, (ny, nx), method=m, precision=p)
+           for (st, nm), (R, C, N, ny, nx, m, sd), p in zip(scenes, SPECS, precs)]
+    # a small wave budget forces several waves per job (slices that do not
+    # start on the 8-row tile grid); a small memory budget forces admission
+    # to wait for earlier jobs to finish
     srv = Server(memory_budget=budget_mb << 20, wave_pixels=2048)
-    tickets = [srv.submit(st, nm, (ny, nx), method=m) for (st, nm), (R, C, N, ny, nx, m, sd) in zip(scenes, SPECS)]
+    tickets = [srv.submit(st, nm, (ny, nx), method=m, precision=p)
+               for (st, nm), (R, C, N, ny, nx, m, sd), p in zip(scenes, SPECS, precs)]
     infos = [srv.wait(t) for t in tickets]
     for t, r in zip(tickets, ref):
         got = srv.result(t)
