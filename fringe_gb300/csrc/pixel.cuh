@@ -345,6 +345,105 @@ __device__ bool warp_chol_c(C2<T> *A, int n, C2<T> *col, int lane)
     return true;
 }
 
+// Two elimination steps per pass (FP32, NP <= 32, row i on lane i): the
+// scaled columns j and j+1 are published together and every row below
+// takes both rank-1 updates in one pass over its entries, as fused
+// multiply-adds.  Same pivot tests and STORE layout as warp_chol_c.  Entries
+// right of the diagonal are left with intermediate values (only the lower
+// triangle and the diagonal are read afterwards).  col: 2 x NP complex.
+template <int LD, int NP, bool STORE = false>
+__device__ bool warp_chol_c2(C2<float> *A, int n, C2<float> *col, int lane)
+{
+    static_assert(NP <= 32, "one row per lane");
+    C2<float> *cA = col, *cB = col + NP;
+    const int i = lane;
+    C2<float> *Ai = A + i * LD;
+    const bool row = i < n;
+    for (int j = 0; j < n; j += 2) {
+        const bool two = (j + 1 < n);
+        const float p1 = A[j * LD + j].x;
+        if (!(p1 > 0.f)) return false;
+        const float r1 = rsqrtf(p1);
+        const bool b1 = row && i > j;
+        C2<float> l1 = cmk<float>(0.f, 0.f);
+        if (b1) {
+            const C2<float> a = Ai[j];
+            l1 = cmk<float>(a.x * r1, a.y * r1);
+        }
+        float r2 = 0.f;
+        C2<float> l2 = cmk<float>(0.f, 0.f);
+        const bool b2 = row && i > j + 1;
+        if (two) {
+            // pivot j+1 after the step-j update: a_(j+1)(j+1) - |l_(j+1)|^2
+            const C2<float> ln = cmk<float>(__shfl_sync(0xffffffffu, l1.x, j + 1), __shfl_sync(0xffffffffu, l1.y, j + 1));
+            const float p2 = fmaf(-ln.y, ln.y, fmaf(-ln.x, ln.x, A[(j + 1) * LD + j + 1].x));
+            if (!(p2 > 0.f)) return false;
+            r2 = rsqrtf(p2);
+            if (b2) {
+                C2<float> a = Ai[j + 1];                    // a - l_i conj(l_(j+1))
+                a.x = fmaf(-l1.x, ln.x, fmaf(-l1.y, ln.y, a.x));
+                a.y = fmaf(-l1.y, ln.x, fmaf(l1.x, ln.y, a.y));
+                l2 = cmk<float>(a.x * r2, a.y * r2);
+            }
+        }
+        if (i < NP) {
+            cA[i] = l1;
+            cB[i] = l2;
+        }
+        if (STORE) {
+            if (i == j) Ai[j] = cmk<float>(r1, 0.f);
+            else if (b1) Ai[j] = l1;
+            if (two) {
+                if (i == j + 1) Ai[j + 1] = cmk<float>(r2, 0.f);
+                else if (b2) Ai[j + 1] = l2;
+            }
+        }
+        __syncwarp();
+        if (b2) {
+            // a_ik -= l1_i conj(l1_k) + l2_i conj(l2_k), k in (j+1, i]
+            for (int k0 = (j + 2) & ~3; k0 <= i; k0 += 4) {
+                const float4 a01 = *reinterpret_cast<const float4 *>(cA + k0);
+                const float4 a23 = *reinterpret_cast<const float4 *>(cA + k0 + 2);
+                const float4 c01 = *reinterpret_cast<const float4 *>(cB + k0);
+                const float4 c23 = *reinterpret_cast<const float4 *>(cB + k0 + 2);
+                const float la[8] = {a01.x, a01.y, a01.z, a01.w, a23.x, a23.y, a23.z, a23.w};
+                const float lb[8] = {c01.x, c01.y, c01.z, c01.w, c23.x, c23.y, c23.z, c23.w};
+                C2<float> x[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) x[u] = Ai[k0 + u];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float ax = la[2 * u], ay = la[2 * u + 1], bx = lb[2 * u], by = lb[2 * u + 1];
+                    x[u].x = fmaf(-l1.x, ax, x[u].x);
+                    x[u].x = fmaf(-l1.y, ay, x[u].x);
+                    x[u].x = fmaf(-l2.x, bx, x[u].x);
+                    x[u].x = fmaf(-l2.y, by, x[u].x);
+                    x[u].y = fmaf(-l1.y, ax, x[u].y);
+                    x[u].y = fmaf(l1.x, ay, x[u].y);
+                    x[u].y = fmaf(-l2.y, bx, x[u].y);
+                    x[u].y = fmaf(l2.x, by, x[u].y);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (k0 + u > j + 1) Ai[k0 + u] = x[u];
+            }
+        }
+        __syncwarp();
+    }
+    return true;
+}
+
+// The Cholesky factorisation used by the solvers: the two-step form for
+// FP32 with one row per lane, else warp_chol_c.  col: 2 x NP complex.
+template <typename T, int LD, int NP, bool STORE = false>
+__device__ __forceinline__ bool warp_chol_any(C2<T> *A, int n, C2<T> *col, int lane)
+{
+    if constexpr (sizeof(T) == 4 && NP <= 32)
+        return warp_chol_c2<LD, NP, STORE>(A, n, col, lane);
+    else
+        return warp_chol_c<T, LD, NP, STORE>(A, n, col, lane);
+}
+
 // Solves (L L^H) x = b with the factor of warp_chol_c<STORE> (1/L_jj on the
 // diagonal).  b / x are lane-distributed (element i on lane i%32, slot i/32).
 template <typename T, int LD, int NP>
@@ -360,8 +459,8 @@ __device__ void warp_chol_solve(const C2<T> *L, int n, C2<T> &b0, C2<T> &b1, int
         y = cscale(y, L[j * LD + j].x);
         if (i0 == j) b0 = y;
         if (NP > 32 && i1 == j) b1 = y;
-        if (i0 > j && i0 < n) b0 = csub(b0, cmul(L[i0 * LD + j], y));
-        if (NP > 32 && i1 > j && i1 < n) b1 = csub(b1, cmul(L[i1 * LD + j], y));
+        if (i0 > j && i0 < n) fms_mul(b0, L[i0 * LD + j], y);
+        if (NP > 32 && i1 > j && i1 < n) fms_mul(b1, L[i1 * LD + j], y);
     }
     // backward: L^H x = y
     for (int j = n - 1; j >= 0; --j) {
@@ -373,8 +472,8 @@ __device__ void warp_chol_solve(const C2<T> *L, int n, C2<T> &b0, C2<T> &b1, int
         if (i0 == j) b0 = x;
         if (NP > 32 && i1 == j) b1 = x;
         // b_i -= conj(L_ji) x_j for i < j
-        if (i0 < j) b0 = csub(b0, ccmul(L[j * LD + i0], x));
-        if (NP > 32 && i1 < j) b1 = csub(b1, ccmul(L[j * LD + i1], x));
+        if (i0 < j) fms_cmul(b0, L[j * LD + i0], x);
+        if (NP > 32 && i1 < j) fms_cmul(b1, L[j * LD + i1], x);
     }
 }
 
@@ -403,7 +502,7 @@ __device__ int lam_min_test_c(const CP &cp, C2<T> *W, C2<T> *col, int n, T thr, 
         __syncwarp();
         for (int i = lane; i < n; i += 32) W[i * LD + i].x -= sh;
         __syncwarp();
-        bool ok = warp_chol_c<T, LD, NP>(W, n, col, lane);
+        bool ok = warp_chol_any<T, LD, NP>(W, n, col, lane);
         __syncwarp();
         if (nsh == 1) return ok ? 1 : -1;
         if (s == 0 && ok) return 1;
@@ -934,7 +1033,7 @@ __device__ int warp_inverse_iteration(C2<T> *W, int n, T sigma, unsigned char *s
     C2<T> *col = reinterpret_cast<C2<T> *>(sm + L::ww);
     for (int i = lane; i < n; i += 32) W[i * LD + i].x -= sigma;
     __syncwarp();
-    if (!warp_chol_c<T, LD, NP, true>(W, n, col, lane)) return -1;
+    if (!warp_chol_any<T, LD, NP, true>(W, n, col, lane)) return -1;
     const T tol = (sizeof(T) == 4) ? T(1e-5) : T(1e-12);
     T rprev = T(-1), cprev = T(1), gap_good = T(0);
     for (int it = 0; it < 10; ++it) {
