@@ -576,8 +576,8 @@ __device__ bool warp_sweep_inverse(T *A, int n, T *rowk, T *inf_norm, int lane)
 // at step k lane k publishes its row (which is also column k) to a shared
 // buffer and every lane updates its own row from it, so the matrix is read
 // from shared memory once and written back once instead of at every step.
-// The arithmetic and its order are those of warp_sweep_inverse.  rowb: 2 x NP
-// floats of shared memory (16-byte aligned).
+// Same sweep as warp_sweep_inverse; the pivot row's update is written
+// x + (1/p - 1) x.  rowb: 2 x NP floats of shared memory (16-byte aligned).
 template <int LD, int NP>
 __device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf_norm, int lane)
 {
@@ -596,17 +596,18 @@ __device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf
         if (!(p > 0.f)) return false;
         const float rp = 1.f / p;
         const bool own = (lane == k);
-        // row k: a_kj / p;  other rows: a_ij - (a_ik / p) a_kj  (a_ik = a_ki)
+        // row k: a_kj / p;  other rows: a_ij - (a_ik / p) a_kj  (a_ik = a_ki).
+        // Lane k published its own row (r = x), so one fused multiply-add
+        // serves both: x + (1/p - 1) x on lane k, x - f r elsewhere.
         const float f = ((lane < NP) ? rk[lane] : 0.f) * rp;
-        const float am = own ? 0.f : 1.f;
-        const float bm = own ? rp : -f;
+        const float bm = own ? rp - 1.f : -f;
 #pragma unroll
         for (int j = 0; j < NP; j += 4) {
             const float4 r = *reinterpret_cast<const float4 *>(rk + j);
-            x[j] = fmaf(bm, r.x, am * x[j]);
-            x[j + 1] = fmaf(bm, r.y, am * x[j + 1]);
-            x[j + 2] = fmaf(bm, r.z, am * x[j + 2]);
-            x[j + 3] = fmaf(bm, r.w, am * x[j + 3]);
+            x[j] = fmaf(bm, r.x, x[j]);
+            x[j + 1] = fmaf(bm, r.y, x[j + 1]);
+            x[j + 2] = fmaf(bm, r.z, x[j + 2]);
+            x[j + 3] = fmaf(bm, r.w, x[j + 3]);
         }
         // column k: x[k] = own ? -1/p : a_ik / p (k is a loop variable, so
         // the register is chosen by block of 8)

@@ -21,10 +21,12 @@ mkdir -p "$HERE/_ref"
 LAPACK_DEFS="-Dzheevr_=scipy_zheevr_ -Dzpotrf_=scipy_zpotrf_ -Dzpotri_=scipy_zpotri_"
 gcc -O2 -fPIC -fopenmp -ffp-contract=off -fcx-limited-range -DFPL_BACKEND_REF \
     -c "$HERE/fpl_oracle.c" -o "$HERE/_ref/fpl_oracle_ref.o"
-g++ -O2 -fPIC -std=c++11 $LAPACK_DEFS -I"$REF/include" \
+gcc -O2 -fPIC -fopenmp -ffp-contract=off -fcx-limited-range -DFPL_BACKEND_REF \
+    -c "$HERE/fpl_nmap_oracle.c" -o "$HERE/_ref/fpl_nmap_oracle_ref.o"
+g++ -O2 -fPIC -std=c++11 $LAPACK_DEFS -I"$REF/include" -I"$REF/src/nmap" \
     -c "$HERE/ref_backend.cpp" -o "$HERE/_ref/ref_backend.o"
 g++ -shared -fopenmp -o "$HERE/_ref/libfpl_ref.so" \
-    "$HERE/_ref/fpl_oracle_ref.o" "$HERE/_ref/ref_backend.o" \
+    "$HERE/_ref/fpl_oracle_ref.o" "$HERE/_ref/fpl_nmap_oracle_ref.o" "$HERE/_ref/ref_backend.o" \
     -L"$SCIPY_LIBS" -l:$(basename "$OPENBLAS") -Wl,-rpath,"$SCIPY_LIBS"
-rm -f "$HERE/_ref/fpl_oracle_ref.o" "$HERE/_ref/ref_backend.o"
+rm -f "$HERE/_ref/fpl_oracle_ref.o" "$HERE/_ref/fpl_nmap_oracle_ref.o" "$HERE/_ref/ref_backend.o"
 echo "built $HERE/_ref/libfpl_ref.so (LAPACK: $(basename "$OPENBLAS"))"

@@ -74,6 +74,26 @@ int fpl_oracle_eig_index(int n, double *A, int index, int want_vec,
  * Returns 0 or the 1-based order of the first non-positive pivot. */
 int fpl_oracle_pd_inverse(int n, double *A);
 
+/* ---- SHP neighbourhood map (fpl_nmap_oracle.c) ---------------------------
+ * The in-memory core of the nmap module (src/nmap/nmap.cpp:345-473) with
+ * the two-sample Kolmogorov-Smirnov test.  stack as above; mask optional
+ * [rows][cols] (0 = excluded); amp_const optional per-band amplitude
+ * calibration constants (the "amplitudeConstant" item of each band, <= 0 or
+ * NULL meaning 1); nmap [rows][cols][nulong] in the Ulongmask layout; count
+ * optional [rows][cols] (set bits, centre included).  Returns 0 or -1. */
+typedef struct {
+    int rows, cols, nbands;
+    int ny, nx;               /* half windows (lines, pixels) */
+    double prob;              /* similarity threshold (nmapOptions::prob) */
+    int nthreads;             /* <= 0: OpenMP default */
+} fpl_nmap_params;
+
+int fpl_oracle_nmap(const fpl_nmap_params *p, const float *stack, const uint8_t *mask,
+                    const double *amp_const, uint32_t *nmap, int32_t *count);
+
+/* The probability of one two-sample test of ascending arrays of length n. */
+double fpl_oracle_ks2(int n, const float *a, const float *b);
+
 /* Which primitive provider this build uses: "port" or "reference". */
 const char *fpl_oracle_kind(void);
 
