@@ -6,10 +6,12 @@ temporal coherence) runs as CUDA kernels behind the C ABI declared in
 ``include/fringe_gb300.h``.  Python entry points:
 
 * ``phase_link(stack, nmap, half_window, ...)`` -- in-memory run;
+* ``nmap(stack, half_window, prob=0.05, ...)`` -- the SHP bitmask (nmap
+  module, two-sample KS test) that phase linking consumes;
 * ``evdlib.Evd`` / ``phase_linklib.Phaselink`` -- drop-in replacements of the
   reference's module wrappers (file level);
 * ``synth`` -- seeded synthetic stacks and SHP bitmasks.
 """
-from .linker import phase_link  # noqa: F401
+from .linker import nmap, phase_link  # noqa: F401
 
-__all__ = ["phase_link"]
+__all__ = ["phase_link", "nmap"]

@@ -36,6 +36,14 @@ class FplStats(ctypes.Structure):
                 ("kernel_ms", ctypes.c_float), ("total_ms", ctypes.c_float)]
 
 
+class FplNmapJob(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int), ("cols", ctypes.c_int), ("nbands", ctypes.c_int),
+                ("half_window_y", ctypes.c_int), ("half_window_x", ctypes.c_int),
+                ("prob", ctypes.c_double), ("memory", ctypes.c_int),
+                ("stack", ctypes.c_void_p), ("mask", ctypes.c_void_p), ("amp_const", ctypes.c_void_p),
+                ("nmap", ctypes.c_void_p), ("count", ctypes.c_void_p)]
+
+
 class FplServerConfig(ctypes.Structure):
     _fields_ = [("memory_budget", ctypes.c_size_t), ("wave_pixels", ctypes.c_longlong),
                 ("device", ctypes.c_int)]
@@ -90,6 +98,7 @@ _SIGS = {
                                        ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_int)]),
     "fpl_ctx_profile_kernels": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "fpl_nmap": (ctypes.c_int, [_P, ctypes.POINTER(FplNmapJob)]),
 }
 _EXTRA = {}
 

@@ -19,7 +19,8 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr"] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC"]
 
-SOURCES = ["api.cu", "kernels_f32.cu", "kernels_f64.cu", "gram_box.cu", "batch.cu", "serve.cu", "noalloc.cu", "io.cpp"]
+SOURCES = ["api.cu", "kernels_f32.cu", "kernels_f64.cu", "gram_box.cu", "batch.cu", "serve.cu", "noalloc.cu",
+           "nmap.cu", "io.cpp"]
 
 
 def _nvcc():

@@ -161,7 +161,8 @@ int fpl_ctx_destroy(fpl_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
     void *bufs[] = {ctx->d_stack, ctx->d_nmap, ctx->d_phase, ctx->d_tcorr, ctx->d_comp,
-                    ctx->d_status, ctx->d_fb_list, ctx->d_small, ctx->d_cbuf, ctx->d_cinfo};
+                    ctx->d_status, ctx->d_fb_list, ctx->d_small, ctx->d_cbuf, ctx->d_cinfo,
+                    ctx->d_nm};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);

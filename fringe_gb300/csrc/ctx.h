@@ -30,6 +30,9 @@ struct fpl_ctx {
     // mixed form: packed coherence matrices of one chunk of rows
     void *d_cbuf = nullptr, *d_cinfo = nullptr;
     size_t cap_cbuf = 0, cap_cinfo = 0;
+    // nmap: sorted amplitudes, validity and staging of host jobs
+    void *d_nm = nullptr;
+    size_t cap_nm = 0;
     // tuning
     float amb_scale = kDefaultAmbScale;
     float cond_max = kDefaultCondMax;

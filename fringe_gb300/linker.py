@@ -151,3 +151,46 @@ class PhaseLinkBatch:
             self.close()
         except Exception:
             pass
+
+
+def nmap(stack, half_window, prob=0.05, mask=None, amp_const=None, device=0, out=None, ctx=None):
+    """SHP neighbourhood map of a stack (the nmap module, KS2 method).
+
+    stack : complex64 [nbands, rows, cols], NumPy (host) or CUDA torch tensor.
+    half_window : (Ny, Nx).  prob: similarity threshold (nmapOptions::prob).
+    mask : optional uint8 [rows, cols] (0 = excluded); amp_const: optional
+    per-band amplitude calibration constants.  Returns dict(nmap uint32
+    [rows, cols, nulong] (int32 for torch), count int32 [rows, cols]).
+    """
+    ny, nx = half_window
+    ctx = ctx or _lib.context(device)
+    lib = _lib.load()
+    nul = ((2 * ny + 1) * (2 * nx + 1) + 31) // 32
+    a = None if amp_const is None else np.ascontiguousarray(amp_const, dtype=np.float64)
+    if _is_torch(stack):
+        import torch
+        if not stack.is_cuda:
+            raise ValueError("torch inputs must be CUDA tensors (use NumPy for host memory)")
+        stack = stack.contiguous()
+        nb, R, C = stack.shape
+        if out is None:
+            out = {"nmap": torch.zeros((R, C, nul), dtype=torch.int32, device=stack.device),
+                   "count": torch.zeros((R, C), dtype=torch.int32, device=stack.device)}
+        m = None if mask is None else mask.contiguous()
+        job = _lib.FplNmapJob(R, C, nb, ny, nx, float(prob), _lib.FPL_MEM_DEVICE, stack.data_ptr(),
+                              m.data_ptr() if m is not None else None,
+                              a.ctypes.data if a is not None else None,
+                              out["nmap"].data_ptr(), out["count"].data_ptr())
+        _lib.check(lib.fpl_nmap(ctx.handle, ctypes.byref(job)), ctx.handle)
+        return out
+    stack = np.ascontiguousarray(stack, dtype=np.complex64)
+    nb, R, C = stack.shape
+    if out is None:
+        out = {"nmap": np.zeros((R, C, nul), np.uint32), "count": np.zeros((R, C), np.int32)}
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+    job = _lib.FplNmapJob(R, C, nb, ny, nx, float(prob), _lib.FPL_MEM_HOST, stack.ctypes.data,
+                          m.ctypes.data if m is not None else None,
+                          a.ctypes.data if a is not None else None,
+                          out["nmap"].ctypes.data, out["count"].ctypes.data)
+    _lib.check(lib.fpl_nmap(ctx.handle, ctypes.byref(job)), ctx.handle)
+    return out

@@ -236,6 +236,32 @@ enum fpl_kernel_tag {
 };
 int fpl_ctx_profile_kernels(const fpl_ctx *ctx, double *ms, int count);
 
+/* ---- SHP neighbourhood map (the nmap module) --------------------------------
+ * The producer of the nmap input: for every pixel, the two-sample
+ * Kolmogorov-Smirnov test of its N amplitudes against those of each pixel of
+ * its (2Ny+1) x (2Nx+1) window; the neighbour's bit is set (Ulongmask layout)
+ * when the test's probability is >= prob, and the centre bit of every valid
+ * pixel.  A pixel is valid when the optional mask is nonzero and all its
+ * amplitudes |x_b| / alpha_b are nonzero and not NaN, alpha_b being the
+ * band's "amplitudeConstant" normalised to the first band (<= 0 or absent:
+ * 1).  Replaces the in-memory core of nmap_process (src/nmap/nmap.cpp:
+ * 345-473; KS2 method, src/nmap/KS2sample.hpp:96-144).  Returns
+ * FPL_ERR_OPTIONS when prob lies within rounding of one of the test's
+ * discrete probability values for this stack depth (move it by 1e-12). */
+typedef struct {
+    int rows, cols, nbands;
+    int half_window_y, half_window_x;    /* nmapOptions::Ny, Nx (default 5, 5) */
+    double prob;                         /* nmapOptions::prob (default 0.05) */
+    int memory;                          /* enum fpl_memory */
+    const void *stack;                   /* complex64 [nbands][rows][cols]        */
+    const uint8_t *mask;                 /* optional [rows][cols], 0 = excluded   */
+    const double *amp_const;             /* optional [nbands], host memory        */
+    uint32_t *nmap;                      /* out [rows][cols][nulong]              */
+    int32_t *count;                      /* optional out [rows][cols]: bits set   */
+} fpl_nmap_job;
+
+int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job);
+
 /* ---- file-level module call ------------------------------------------------
  * Mirrors evdOptions (src/evd/evd.hpp:19-54; src/phase_link/phase_link.hpp:20-57)
  * and evd_process(evdOptions*) (src/evd/evd.cpp:16-888;

@@ -34,6 +34,12 @@ class _Params(ctypes.Structure):
         "row_end", "nthreads")]
 
 
+class _NmapParams(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int), ("cols", ctypes.c_int), ("nbands", ctypes.c_int),
+                ("ny", ctypes.c_int), ("nx", ctypes.c_int), ("prob", ctypes.c_double),
+                ("nthreads", ctypes.c_int)]
+
+
 def build_port(force=False):
     """Compile the port library with the committed Makefile."""
     if force or not os.path.exists(PORT_SO):
@@ -72,6 +78,10 @@ def load(kind="port"):
     lib.fpl_oracle_pd_inverse.argtypes = [ctypes.c_int, P]
     lib.fpl_oracle_pd_inverse.restype = ctypes.c_int
     lib.fpl_oracle_kind.restype = ctypes.c_char_p
+    lib.fpl_oracle_nmap.argtypes = [ctypes.POINTER(_NmapParams), P, P, P, P, P]
+    lib.fpl_oracle_nmap.restype = ctypes.c_int
+    lib.fpl_oracle_ks2.argtypes = [ctypes.c_int, P, P]
+    lib.fpl_oracle_ks2.restype = ctypes.c_double
     _LIBS[kind] = lib
     return lib
 
@@ -127,3 +137,37 @@ def pd_inverse(A, kind="port"):
     a = np.asfortranarray(A, dtype=np.complex128).copy(order="F")
     info = lib.fpl_oracle_pd_inverse(n, _ptr(a))
     return info, a
+
+
+def nmap(stack, ny, nx, prob=0.05, mask=None, amp_const=None, nthreads=0, kind="port"):
+    """SHP map of the nmap module (KS2 method) over a whole scene.
+
+    stack: complex64 [nbands, rows, cols]; mask: optional uint8 [rows, cols];
+    amp_const: optional per-band calibration constants.  Returns
+    (nmap uint32 [rows, cols, nulong], count int32 [rows, cols]).
+    """
+    lib = load(kind)
+    stack = np.ascontiguousarray(stack, dtype=np.complex64)
+    nb, R, C = stack.shape
+    nul = ((2 * ny + 1) * (2 * nx + 1) + 31) // 32
+    out = np.zeros((R, C, nul), np.uint32)
+    count = np.zeros((R, C), np.int32)
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+    a = None if amp_const is None else np.ascontiguousarray(amp_const, dtype=np.float64)
+    p = _NmapParams(R, C, nb, ny, nx, float(prob), nthreads)
+    rc = lib.fpl_oracle_nmap(ctypes.byref(p), _ptr(stack), _ptr(m), _ptr(a), _ptr(out), _ptr(count))
+    if rc != 0:
+        raise ValueError("oracle rejected the parameters (%d)" % rc)
+    return out, count
+
+
+def ks2(a, b, kind="port"):
+    """Probability of the two-sample KS test of two equal-length samples
+    (sorted ascending here, as the nmap module sorts them)."""
+    lib = load(kind)
+    a = np.ascontiguousarray(np.sort(np.asarray(a, np.float32)))
+    b = np.ascontiguousarray(np.sort(np.asarray(b, np.float32)))
+    assert a.shape == b.shape
+    pad_a = np.concatenate([a, a[-1:]])     # the reference may read one past the end
+    pad_b = np.concatenate([b, b[-1:]])
+    return lib.fpl_oracle_ks2(len(a), _ptr(pad_a), _ptr(pad_b))
