@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-serve", action="store_true",
                     help="skip the serving-loop measurement")
     ap.add_argument("--serve-jobs", type=int, default=24)
+    ap.add_argument("--no-nmap", action="store_true", help="skip the SHP-map measurement")
     return ap.parse_args()
 
 
@@ -309,6 +310,37 @@ def device_form(phase_link, d_stack, d_nmap, ctx, precision, method, steps, warm
     return {"ms": ms, "kernel_ms": kms, "clocks": clk, "launches_per_step": launches}, out
 
 
+def nmap_measurement(stack, d_stack, ctx, steps, cpu_rows):
+    """The SHP map producer (fpl_nmap, KS2 test) on the same scene: device-
+    resident px/s over `steps` runs (each call ends with a stream sync), and
+    the oracle's restatement of the nmap module on the host cores over a row
+    sample."""
+    import torch
+    from fringe_gb300 import nmap
+    nb, R, C = stack.shape
+    out = None
+    for _ in range(2):
+        out = nmap(d_stack, (NY, NX), ctx=ctx, out=out)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        nmap(d_stack, (NY, NX), ctx=ctx, out=out)
+    dt = (time.perf_counter() - t0) / steps
+    res = {"value": R * C / dt, "unit": "px/s", "ms_per_step": dt * 1e3,
+           "mean_count": float(out["count"].float().mean().item()),
+           "workload": "KS2 threshold 0.05 on the same %dx%d N=%d scene, half-window %dx%d" % (R, C, nb, NY, NX)}
+    if cpu_rows:
+        import oracle
+        rows = min(cpu_rows, R - 2 * NY)
+        t0 = time.perf_counter()
+        oracle.nmap(stack[:, :rows + 2 * NY], NY, NX, 0.05, nthreads=os.cpu_count() or 1)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": rows * C / dt, "unit": "px/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": "%d rows (+%d apron rows) of the scene, %.1f s"
+                                                          % (rows, 2 * NY, dt)}
+    return res
+
+
 def accuracy(out, ref, valid_ref):
     """Phase and coherence error of one form against the FP64 form, over the
     pixels valid in both; validity-code mismatches counted separately."""
@@ -488,6 +520,8 @@ def main():
         line["accuracy_vs_fp64"] = acc
     if not args.no_serve and world == 1:
         line["serving"] = serving_measurement(args.serve_jobs)
+    if not args.no_nmap and world == 1:
+        line["nmap"] = nmap_measurement(stack, d_stack, ctx, max(1, args.steps), 0 if args.no_cpu else 384)
     if not args.no_cpu:
         rows = args.cpu_rows or 480          # about 15 s on 16 host cores
         line["cpu_baseline"] = cpu_baseline(stack, nmap, args.method, min(rows, R))

@@ -1523,6 +1523,8 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
 
     // ---- the eigenvector --------------------------------------------------
     C2<T> z0, z1;
+    T lam = T(0), eig_lo = T(0), eig_hi = T(0), dM = T(0);
+    int eig_index = 0;   // > 0: eigenpair of Wm by this index on the Householder path
     if (mode == 0) {
         // M = inv(|C|) o C (evd.cpp:667); Xr shares bytes with Wm, so each
         // lane reads its inverse row into registers before M is written.
@@ -1554,7 +1556,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         T tr = T(0);
         for (int i = lane; i < n; i += 32) tr += Wm[i * LD + i].x;
         tr = warp_sum(tr) / T(n);
-        const T dM = (fp32 && !plink) ? amb * fro(Wm) : T(0);
+        dM = (fp32 && !plink) ? amb * fro(Wm) : T(0);
         __syncwarp();
         bool done = false;
         if (fp32) {
@@ -1568,40 +1570,41 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             const T sigma = T(0.98) * min(rho0, T(1));
             __syncwarp();
             if (sigma > thr + dM) {
-                T lam, res;
-                int st = warp_inverse_iteration<T, NP>(Wm, n, sigma, sm, lane, z0, z1, &lam, &res);
-                if (st == 0) {
+                // one call site for the iteration and for rebuilding M (the
+                // factorisation consumes it), so each is inlined once
+                T sig = sigma;
+                int st = 0;
+                for (int attempt = 0; attempt < 2; ++attempt) {
+                    T lam, res;
+                    st = warp_inverse_iteration<T, NP>(Wm, n, sig, sm, lane, z0, z1, &lam, &res);
+                    if (st != 1) {
+                        // M for a second shift or for the Householder path
+                        __syncwarp();
+                        abs_inverse();
+                        form_M();
+                    }
+                    if (st != 0 || attempt == 1) break;
                     // slow: shift again just below the current Rayleigh
                     // quotient (lambda_1 >= rho - res when the iterate is
                     // closest to v_1; the Cholesky test verifies the shift)
                     if (lane == 0) atomicAdd(P.slow, 1);
                     const T sigma1 = lam - T(2) * res;
-                    __syncwarp();
-                    abs_inverse();
-                    form_M();
-                    if (sigma1 > sigma && sigma1 > thr + dM)
-                        st = warp_inverse_iteration<T, NP>(Wm, n, sigma1, sm, lane, z0, z1, &lam, &res);
-                    else
+                    if (!(sigma1 > sig && sigma1 > thr + dM)) {
                         st = -1;
+                        break;
+                    }
+                    sig = sigma1;
                 }
-                if (st == 1) {
-                    done = true;   // lambda_1 > sigma > 1e-6 + band: the -7 test passes
-                } else {
-                    __syncwarp();
-                    abs_inverse();  // rebuild M for the Householder path
-                    form_M();
-                }
+                // converged: lambda_1 > sigma > 1e-6 + band, the -7 test passes
+                done = (st == 1);
             }
         }
         if (!done) {
-            const T lam = warp_eigpair<T, NP>(Wm, n, 1, T(-1e30), tr * T(1.0001), sm, lane, z0, z1);
-            if (!plink) {
-                if (fp32 && lam < thr + dM && lam >= thr - dM) { defer_fp64(P, pp, lane); return; }
-                if (lam < thr) { put_code(P, pp, lane, -7); return; }
-            }
+            eig_index = 1;
+            eig_lo = T(-1e30);
+            eig_hi = tr * T(1.0001);
         }
     } else {
-        T lam;
         bool ok = warp_power<T, NP>(cp, n, sm, lane, z0, z1, &lam);
         if (!ok) {
             if (lane == 0 && fp32) atomicAdd(P.slow, 1);
@@ -1618,8 +1621,19 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
                 }
             }
             __syncwarp();
-            lam = warp_eigpair<T, NP>(Wm, n, n, T(0.999), T(1e30), sm, lane, z0, z1);
+            eig_index = n;
+            eig_lo = T(0.999);
+            eig_hi = T(1e30);
         }
+    }
+    // Householder path, one call site for both methods
+    if (eig_index) lam = warp_eigpair<T, NP>(Wm, n, eig_index, eig_lo, eig_hi, sm, lane, z0, z1);
+    if (mode == 0) {
+        if (eig_index && !plink) {
+            if (fp32 && lam < thr + dM && lam >= thr - dM) { defer_fp64(P, pp, lane); return; }
+            if (lam < thr) { put_code(P, pp, lane, -7); return; }
+        }
+    } else {
         // trace(C) = n, so lambda_max >= 1: the -7 test of evd.cpp:718-726
         // cannot trigger for a finite C.
         if (!plink && lam < thr) { put_code(P, pp, lane, -7); return; }
