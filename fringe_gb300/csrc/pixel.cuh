@@ -1377,6 +1377,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
     // |C| into Xr (unit diagonal), then its sweep inverse.  Returns
     // +1 inverted (X = inv|C| in Xr), -1 not positive definite, 0 undecided
     // in FP32 (rounding band or condition too large).
+    T xnorm = T(0);     // inf-norm of inv|C| from the last abs_inverse()
     auto abs_inverse = [&]() -> int {
         T rs = T(0);
 #pragma unroll
@@ -1402,7 +1403,6 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         }
         const T anorm = warp_max(rs);          // |C| inf-norm
         __syncwarp();
-        T xnorm;
         bool ok;
         if constexpr (sizeof(T) == 4 && NP <= 32)
             ok = warp_sweep_inverse_rows<LD, NP>(reinterpret_cast<float *>(Xr), nn,
@@ -1415,25 +1415,35 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         return 1;
     };
 
-    if (!plink) {
-        if (P.method == M_MLE) {
-            // evd.cpp:598-686
-            if (npix < n) {
-                // fewer SHPs than dates: Gamma has rank <= npix < n, so its
-                // smallest eigenvalue is 0 up to FP32 product rounding (far
-                // below 1e-6): the reference reports -2.
-                put_code(P, pp, lane, -2);
-                return;
+    const bool mle_evd = !plink && P.method == M_MLE;
+    if (mle_evd) {
+        // evd.cpp:598-686
+        if (npix < n) {
+            // fewer SHPs than dates: Gamma has rank <= npix < n, so its
+            // smallest eigenvalue is 0 up to FP32 product rounding (far
+            // below 1e-6): the reference reports -2.
+            put_code(P, pp, lane, -2);
+            return;
+        }
+        const T dC = fp32 ? amb * fro_c() : T(0);
+        const int r = lam_min_test_c<T, LD, NP>(cp, Wm, col, n, thr, dC, lane);
+        if (r == 0) { defer_fp64(P, pp, lane); return; }
+        if (r < 0) { put_code(P, pp, lane, -2); return; }
+    }
+    if (mle_evd || plink) {
+        // |C| and its inverse: evd.cpp:623-664 (check, then inverse);
+        // phase_link.cpp:540-618 (MLE if |C| is invertible, else EVD).  One
+        // call site for both modules.
+        const int r = abs_inverse();
+        if (r == 0) { defer_fp64(P, pp, lane); return; }
+        if (plink) {
+            if (r > 0) {
+                mode = 0;
+            } else {
+                mode = 1;
+                pstatus = 3;
             }
-            const T dC = fp32 ? amb * fro_c() : T(0);
-            int r = lam_min_test_c<T, LD, NP>(cp, Wm, col, n, thr, dC, lane);
-            if (r == 0) { defer_fp64(P, pp, lane); return; }
-            if (r < 0) { put_code(P, pp, lane, -2); return; }
-            // |C| check (evd.cpp:623-644) and inverse (evd.cpp:652-664).
-            // lambda_min(|C|) >= 1 / ||inv|C|||_inf, so a small inverse norm
-            // settles the 1e-6 test; anything else is settled in FP64.
-            r = abs_inverse();
-            if (r == 0) { defer_fp64(P, pp, lane); return; }
+        } else {
             if (r < 0) {
                 // FP64: not positive definite, so lambda_min(|C|) <= 0 < 1e-6
                 put_code(P, pp, lane, -4);
@@ -1477,48 +1487,33 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
                     abs_inverse();
                 }
             } else {
-                T xn = T(0);
-                for (int i = lane; i < n; i += 32) {
-                    T s = T(0);
-                    for (int j = 0; j < n; ++j) s += abs(Xr[i * LD + j]);
-                    xn = max(xn, s);
-                }
-                xn = warp_max(xn);
+                // lambda_min(|C|) >= 1 / ||inv|C|||_inf, so a small inverse
+                // norm settles the 1e-6 test; anything else is settled in FP64
                 const T dA = amb * T(n);
-                if (!(T(1) / xn > thr + dA)) { defer_fp64(P, pp, lane); return; }
+                if (!(T(1) / xnorm > thr + dA)) { defer_fp64(P, pp, lane); return; }
             }
             mode = 0;
-        } else {
-            if (P.method == M_STBAS) {                       // evd.cpp:695-706
-#pragma unroll
-                for (int h = 0; h < RS::H; ++h) {
-                    const int i = lane + 32 * h;
-#pragma unroll 1
-                    for (int c = 0; c < RS::CH; ++c) {
-                        C2<T> v[8];
-                        cp.load(h, c, v);
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            const int j = 8 * c + k;
-                            if (j - i > P.bw || i - j > P.bw) v[k] = cmk<T>(T(0), T(0));
-                        }
-                        cp.store(h, c, v);
-                    }
-                }
-                cp.fence();
-            }
-            mode = 1;
         }
     } else {
-        // phase_link.cpp:540-618: MLE if |C| is invertible, else EVD
-        int r = abs_inverse();
-        if (r == 0) { defer_fp64(P, pp, lane); return; }
-        if (r > 0) {
-            mode = 0;
-        } else {
-            mode = 1;
-            pstatus = 3;
+        if (P.method == M_STBAS) {                       // evd.cpp:695-706
+#pragma unroll
+            for (int h = 0; h < RS::H; ++h) {
+                const int i = lane + 32 * h;
+#pragma unroll 1
+                for (int c = 0; c < RS::CH; ++c) {
+                    C2<T> v[8];
+                    cp.load(h, c, v);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const int j = 8 * c + k;
+                        if (j - i > P.bw || i - j > P.bw) v[k] = cmk<T>(T(0), T(0));
+                    }
+                    cp.store(h, c, v);
+                }
+            }
+            cp.fence();
         }
+        mode = 1;
     }
 
     // ---- the eigenvector --------------------------------------------------
