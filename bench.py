@@ -72,6 +72,8 @@ def parse():
                     help="skip the serving-loop measurement")
     ap.add_argument("--serve-jobs", type=int, default=24)
     ap.add_argument("--no-nmap", action="store_true", help="skip the SHP-map measurement")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched-ministack and ill-conditioned measurements")
     return ap.parse_args()
 
 
@@ -341,6 +343,106 @@ def nmap_measurement(stack, d_stack, ctx, steps, cpu_rows):
     return res
 
 
+def batch_measurement(stack, nmap, seed=7):
+    """Uneven ministacks in one batched launch sequence (replayed CUDA graph):
+    16 tiles of 512^2..2048^2 pixels cut from the scene, ministacks of
+    N in {10, 15, 20, 30} dates of it and N = 45 from a second 1024^2
+    45-date scene, half-window 5x10, EVD and MLE alternating.  Per form: the
+    batch's px/s, against the same jobs run one after another."""
+    import torch
+    from fringe_gb300 import synth
+    from fringe_gb300.linker import PhaseLinkBatch, phase_link
+    rng = np.random.Generator(np.random.PCG64(seed))
+    st45, nm45 = synth.scene("voronoi", 1024, 1024, 45, NY, NX, seed=1045)
+    d_main = torch.from_numpy(stack).cuda()
+    d_nm = torch.from_numpy(nmap.view(np.int32)).cuda()
+    d45 = torch.from_numpy(st45).cuda()
+    d_nm45 = torch.from_numpy(nm45.view(np.int32)).cuda()
+    R = stack.shape[1]
+    jobs, px = [], 0
+    for k in range(16):
+        if k % 5 == 4:
+            size, n, src, snm = int(rng.choice([512, 1024])), 45, d45, d_nm45
+        else:
+            size, n, src, snm = int(rng.choice([512, 1024, 1536, 2048])), int(rng.choice([10, 15, 20, 30])), d_main, d_nm
+        size = min(size, src.shape[1])
+        r0 = int(rng.integers(0, src.shape[1] - size + 1))
+        c0 = int(rng.integers(0, src.shape[2] - size + 1))
+        jobs.append({"stack": src[:n, r0:r0 + size, c0:c0 + size].contiguous(),
+                     "nmap": snm[r0:r0 + size, c0:c0 + size].contiguous(),
+                     "half_window": (NY, NX), "method": "MLE" if k % 2 else "EVD",
+                     "mini_stack_count": 1 + k % 3})
+        px += size * size
+    res = {"jobs": len(jobs), "pixels": px,
+           "mix": "16 tiles 512^2..2048^2, N in {10,15,20,30,45}, half-window 5x10, EVD/MLE, miniStackCount 1..3"}
+    for prec in ("mixed", "fp32"):
+        b = PhaseLinkBatch(jobs, graph=True, autotune=(prec == "fp32"), precision=prec)
+        for _ in range(2):
+            b.run()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            b.run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+        b.close()
+        # the same jobs one after another (fpl_run_async each)
+        outs = [None] * len(jobs)
+        for k, j in enumerate(jobs):
+            outs[k] = phase_link(j["stack"], j["nmap"], j["half_window"], method=j["method"],
+                                 mini_stack_count=j["mini_stack_count"], precision=prec, out=outs[k])
+        torch.cuda.synchronize()
+        e0.record()
+        for k, j in enumerate(jobs):
+            phase_link(j["stack"], j["nmap"], j["half_window"], method=j["method"],
+                       mini_stack_count=j["mini_stack_count"], precision=prec, out=outs[k])
+        e1.record()
+        torch.cuda.synchronize()
+        ms1 = e0.elapsed_time(e1)
+        res[prec] = {"batch_px_s": px / ms * 1e3, "batch_ms": ms,
+                     "one_by_one_px_s": px / ms1 * 1e3, "one_by_one_ms": ms1}
+    del d45, d_nm45
+    return res
+
+
+def illcond_measurement(ctx):
+    """Ill-conditioned MLE stress (gamma0 ~ U(0.05, 0.9), 10% of pixels with
+    gamma_inf = 0): N = 64, 512^2 pixels (a sub-scene of the 1024^2
+    configuration), half-window 5x10: px/s and error of the mixed form
+    against the FP64 form, and the share of pixels settled in FP64."""
+    import torch
+    from fringe_gb300 import phase_link, synth
+    st, nm = synth.scene("illcond", 512, 512, 64, NY, NX, seed=1003)
+    d, dn = torch.from_numpy(st).cuda(), torch.from_numpy(nm.view(np.int32)).cuda()
+    out = None
+    for _ in range(2):
+        out = phase_link(d, dn, (NY, NX), method="MLE", precision="mixed", ctx=ctx, out=out)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        phase_link(d, dn, (NY, NX), method="MLE", precision="mixed", ctx=ctx, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 3
+    # fp64-settled count of one run on the context's stream
+    h = phase_link(st, nm, (NY, NX), method="MLE", precision="mixed", ctx=ctx)
+    fp64_px = ctx.stats()["fp64_pixels"]
+    ref = {k: torch.zeros_like(v) for k, v in out.items()}
+    ctx.set_tuning(force_fp64=True)
+    phase_link(d, dn, (NY, NX), method="MLE", ctx=ctx, out=ref)
+    torch.cuda.synchronize()
+    ctx.set_tuning(force_fp64=False)
+    acc = accuracy(out, ref, ref["tcorr"] > 0)
+    return {"workload": "illcond 512x512 N=64 half-window 5x10 MLE (mixed form)",
+            "value": 512 * 512 / ms * 1e3, "unit": "px/s", "ms": ms,
+            "fp64_settled_px": int(fp64_px), "accuracy_vs_fp64": acc}
+
+
 def accuracy(out, ref, valid_ref):
     """Phase and coherence error of one form against the FP64 form, over the
     pixels valid in both; validity-code mismatches counted separately."""
@@ -520,6 +622,9 @@ def main():
         line["accuracy_vs_fp64"] = acc
     if not args.no_serve and world == 1:
         line["serving"] = serving_measurement(args.serve_jobs)
+    if not args.no_batch and world == 1:
+        line["batch"] = batch_measurement(stack, nmap)
+        line["illconditioned"] = illcond_measurement(ctx)
     if not args.no_nmap and world == 1:
         line["nmap"] = nmap_measurement(stack, d_stack, ctx, max(1, args.steps), 0 if args.no_cpu else 384)
     if not args.no_cpu:

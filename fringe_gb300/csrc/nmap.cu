@@ -139,8 +139,11 @@ __global__ void __launch_bounds__(256) k_nmap_ks(NmapParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int HW = NM_TC + 2 * P.nx, HH = P.tr + 2 * P.ny, HP = HW * HH;
-    float *S = reinterpret_cast<float *>(smem);                       // [nb][HP]
-    uint8_t *V = smem + sizeof(float) * (size_t)P.nb * HP;           // [HP]
+    // odd stride between dates: lanes whose merge walks sit at different
+    // positions spread over the banks
+    const int SP = HP | 1;
+    float *S = reinterpret_cast<float *>(smem);                       // [nb][SP]
+    uint8_t *V = smem + sizeof(float) * (size_t)P.nb * SP;           // [HP]
     const int ntc = (P.cols + NM_TC - 1) / NM_TC;
     const int R0 = (blockIdx.x / ntc) * P.tr, C0 = (blockIdx.x % ntc) * NM_TC;
     const int tid = threadIdx.x, nth = blockDim.x;
@@ -156,7 +159,7 @@ __global__ void __launch_bounds__(256) k_nmap_ks(NmapParams P)
         const int hr = h / HW, hc = h - hr * HW;
         const int r = R0 - P.ny + hr, c = C0 - P.nx + hc;
         const bool in = r >= 0 && r < P.rows && c >= 0 && c < P.cols;
-        S[e] = in ? __ldg(P.sorted + b * P.plane + (long long)r * P.cols + c) : 0.f;
+        S[b * SP + h] = in ? __ldg(P.sorted + b * P.plane + (long long)r * P.cols + c) : 0.f;
     }
     __syncthreads();
     const int tr = tid / NM_TC, tc = tid % NM_TC;
@@ -178,7 +181,7 @@ __global__ void __launch_bounds__(256) k_nmap_ks(NmapParams P)
                 if (hq == hp) {
                     set = true;                                  // the centre (nmap.cpp:441-445)
                 } else {
-                    const int D = ks_steps(S + hp, S + hq, HP, P.nb);
+                    const int D = ks_steps(S + hp, S + hq, SP, P.nb);
                     set = (D < 64) ? ((P.pass_lo >> D) & 1ull) != 0 : (P.pass_hi & 1u) != 0;
                 }
             }
@@ -250,8 +253,8 @@ int nm_tile_rows(int nb, int ny, int nx, size_t *smem)
     const size_t per_row = (size_t)HW * (sizeof(float) * nb + 1);
     const size_t budget = 200 * 1024;
     int tr = 8;
-    while (tr > 1 && per_row * (tr + 2 * ny) > budget) --tr;
-    *smem = per_row * (tr + 2 * ny);
+    while (tr > 1 && per_row * (tr + 2 * ny) + sizeof(float) * nb > budget) --tr;
+    *smem = per_row * (tr + 2 * ny) + sizeof(float) * nb;        // + the odd-stride pad per date
     return *smem <= 227 * 1024 ? tr : 0;
 }
 
