@@ -148,7 +148,8 @@ int fpl_ctx_create(int device, fpl_ctx **out)
     if (e != cudaSuccess) { delete ctx; return cuda_fail(nullptr, e, "cudaStreamCreate"); }
     cudaEventCreate(&ctx->ev0);
     cudaEventCreate(&ctx->ev1);
-    e = cudaMalloc(&ctx->d_small, 256);
+    cudaEventCreateWithFlags(&ctx->ev_last, cudaEventDisableTiming);
+    e = cudaMalloc(&ctx->d_small, kCounterBlock * kRunChunks);
     if (e != cudaSuccess) { fpl_ctx_destroy(ctx); return cuda_fail(nullptr, e, "cudaMalloc"); }
     *out = ctx;
     return FPL_OK;
@@ -160,11 +161,15 @@ int fpl_ctx_destroy(fpl_ctx *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->chunk_ev) cudaEventDestroy(e);
+    if (ctx->s_in) cudaStreamDestroy(ctx->s_in);
+    if (ctx->s_out) cudaStreamDestroy(ctx->s_out);
     void *bufs[] = {ctx->d_stack, ctx->d_nmap, ctx->d_phase, ctx->d_tcorr, ctx->d_comp,
                     ctx->d_status, ctx->d_fb_list, ctx->d_small, ctx->d_cbuf, ctx->d_cinfo,
                     ctx->d_nm};
     for (void *b : bufs)
         if (b) cudaFree(b);
+    if (ctx->ev_last) cudaEventDestroy(ctx->ev_last);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -181,11 +186,36 @@ int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out)
 
 }  // extern "C"
 
+static int fpl_enqueue_body(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
+                            void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
+                            bool fp64_all, void *counters, bool count_run);
+
 // Enqueues both passes on `st` for device buffers.  Scratch: the context's
 // work-list buffer (grown with cudaMalloc when too small) and d_small.
 int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
                 void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
-                bool fp64_all)
+                bool fp64_all, void *counters, bool count_run)
+{
+    if (!counters) counters = ctx->d_small;
+    // runs sharing this context share its scratch: a run waits for the
+    // previous one, whatever stream it was enqueued on (not while capturing,
+    // where the graph orders the work)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    FPL_CUDA(ctx, cudaStreamIsCapturing(st, &cap));
+    const bool order = (cap == cudaStreamCaptureStatusNone);
+    if (order && ctx->last_used) FPL_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_last, 0));
+    int rc_ = fpl_enqueue_body(ctx, job, stack, nmap, phase, tcorr, comp, status, st, fp64_all, counters, count_run);
+    if (rc_) return rc_;
+    if (order) {
+        FPL_CUDA(ctx, cudaEventRecord(ctx->ev_last, st));
+        ctx->last_used = true;
+    }
+    return FPL_OK;
+}
+
+static int fpl_enqueue_body(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
+                            void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
+                            bool fp64_all, void *counters, bool count_run)
 {
     const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
     int rc = 0;
@@ -215,18 +245,18 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
     P.min_neigh = job->min_neighbors;
     P.amb = ctx->amb_scale;
     P.cond_max = ctx->cond_max;
-    int *d_count = reinterpret_cast<int *>(ctx->d_small);
-    unsigned *d_err = reinterpret_cast<unsigned *>(static_cast<char *>(ctx->d_small) + 16);
+    int *d_count = reinterpret_cast<int *>(counters);
+    unsigned *d_err = reinterpret_cast<unsigned *>(static_cast<char *>(counters) + 16);
     P.fb_count = d_count;
     P.err = d_err;
-    P.slow = reinterpret_cast<int *>(static_cast<char *>(ctx->d_small) + 32);
+    P.slow = reinterpret_cast<int *>(static_cast<char *>(counters) + 32);
     // work list: at most one entry per pixel of the range
     size_t need = sizeof(long long) * (size_t)(P.npix > 0 ? P.npix : 1);
     rc = grow(ctx, &ctx->d_fb_list, &ctx->cap_fb_list, need);
     if (rc) return rc;
     P.fb_list = static_cast<long long *>(ctx->d_fb_list);
     P.fb_cap = (int)(P.npix < 0x7fffffff ? P.npix : 0x7fffffff);
-    FPL_CUDA(ctx, cudaMemsetAsync(ctx->d_small, 0, 64, st));
+    FPL_CUDA(ctx, cudaMemsetAsync(counters, 0, kCounterBlock, st));
     if (P.npix == 0) return FPL_OK;
     if (fp64_all) {
         KParams Q = P;
@@ -251,7 +281,7 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
         ctx->prof_tag.push_back(tag);
         return cudaSuccess;
     };
-    if (ctx->profile) ctx->prof_runs++;
+    if (ctx->profile && count_run) ctx->prof_runs++;
     const bool mixed = job->precision == FPL_PREC_MIXED && fpl::gram_box_supported(P.nb, P.ny, P.nx);
     if (mixed) {
         // tensor-core Gamma records, then eigen-solves, chunk by chunk of
@@ -308,9 +338,15 @@ int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream)
     // the stream is used as given: NULL is the legacy default stream
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     return fpl_enqueue(ctx, job, job->stack, job->nmap, job->phase, job->tcorr, job->comp,
-                       job->status, st, ctx->force_fp64);
+                       job->status, st, ctx->force_fp64, ctx->d_small, true);
 }
 
+// Host-memory jobs run in row chunks so that copies overlap the compute:
+// chunk c's stack rows (with the window apron and the rows of its first and
+// last 8-row tiles) and nmap rows go up on a copy stream, the chunk is
+// computed on the context's stream once they have arrived, and its outputs
+// come back on a third stream while the next chunk computes.  Each chunk has
+// its own block of counters so the statistics add up over the run.
 int fpl_run(fpl_ctx *ctx, const fpl_job *job)
 {
     if (!ctx) return FPL_ERR_NULL;
@@ -319,64 +355,105 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job)
     auto t0 = std::chrono::steady_clock::now();
     FPL_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
-    const size_t plane = (size_t)job->rows * job->cols;
+    const int rows = job->rows, cols = job->cols, nb = job->nbands, ny = job->half_window_y;
+    const size_t plane = (size_t)rows * cols;
     const int nulong = ((2 * job->half_window_y + 1) * (2 * job->half_window_x + 1) + 31) / 32;
-    const size_t b_stack = plane * job->nbands * 8, b_nmap = plane * nulong * 4;
+    const size_t b_stack = plane * nb * 8, b_nmap = plane * nulong * 4;
     const size_t b_tc = plane * 4, b_comp = plane * 8, b_st = plane * 4;
-    const void *stack = job->stack;
-    const uint32_t *nmap = job->nmap;
-    void *phase = job->phase, *comp = job->comp;
-    float *tcorr = job->tcorr;
-    int32_t *status = job->status;
-    if (job->memory == FPL_MEM_HOST) {
+    const int r0 = job->row_begin, r1 = job->row_end <= 0 ? rows : job->row_end;
+    int nchunks = 1;
+    if (job->memory == FPL_MEM_DEVICE) {
+        FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+        rc = fpl_enqueue(ctx, job, job->stack, job->nmap, job->phase, job->tcorr, job->comp, job->status, st,
+                         ctx->force_fp64, ctx->d_small, true);
+        if (rc) return rc;
+        FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+    } else {
         if ((rc = grow(ctx, &ctx->d_stack, &ctx->cap_stack, b_stack))) return rc;
         if ((rc = grow(ctx, &ctx->d_nmap, &ctx->cap_nmap, b_nmap))) return rc;
         if ((rc = grow(ctx, &ctx->d_phase, &ctx->cap_phase, b_stack))) return rc;
         if ((rc = grow(ctx, &ctx->d_tcorr, &ctx->cap_tcorr, b_tc))) return rc;
         if ((rc = grow(ctx, &ctx->d_comp, &ctx->cap_comp, b_comp))) return rc;
         if (job->status && (rc = grow(ctx, &ctx->d_status, &ctx->cap_status, b_st))) return rc;
-        FPL_CUDA(ctx, cudaMemcpyAsync(ctx->d_stack, job->stack, b_stack, cudaMemcpyHostToDevice, st));
-        FPL_CUDA(ctx, cudaMemcpyAsync(ctx->d_nmap, job->nmap, b_nmap, cudaMemcpyHostToDevice, st));
-        stack = ctx->d_stack;
-        nmap = static_cast<const uint32_t *>(ctx->d_nmap);
-        phase = ctx->d_phase;
-        tcorr = static_cast<float *>(ctx->d_tcorr);
-        comp = ctx->d_comp;
-        status = job->status ? static_cast<int32_t *>(ctx->d_status) : nullptr;
+        if (!ctx->s_in) FPL_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_in, cudaStreamNonBlocking));
+        if (!ctx->s_out) FPL_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking));
+        while (ctx->chunk_ev.size() < 2 * (size_t)kRunChunks) {
+            cudaEvent_t e;
+            FPL_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            ctx->chunk_ev.push_back(e);
+        }
+        char *d_stack = static_cast<char *>(ctx->d_stack);
+        char *d_phase = static_cast<char *>(ctx->d_phase);
+        char *d_comp = static_cast<char *>(ctx->d_comp);
+        uint32_t *d_nmap = static_cast<uint32_t *>(ctx->d_nmap);
+        float *d_tcorr = static_cast<float *>(ctx->d_tcorr);
+        int32_t *d_status = job->status ? static_cast<int32_t *>(ctx->d_status) : nullptr;
+        const char *h_stack = static_cast<const char *>(job->stack);
+        int step = (r1 - r0 + kRunChunks - 1) / kRunChunks;
+        step = std::max(8, (step + 7) & ~7);
+        nchunks = std::max(1, (r1 - r0 + step - 1) / step);
+        int copied = std::max(0, r0 / 8 * 8 - ny);     // first stack row on the device
+        FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+        for (int c = 0; c < nchunks; ++c) {
+            const int a = r0 + c * step, b = std::min(r1, a + step);
+            if (b <= a) continue;
+            // stack rows every computed pixel's window (and the chunk's tiles) read
+            const int need = std::min(rows, (b + 7) / 8 * 8 + ny);
+            if (need > copied) {
+                const size_t off = (size_t)copied * cols * 8;
+                FPL_CUDA(ctx, cudaMemcpy2DAsync(d_stack + off, plane * 8, h_stack + off, plane * 8,
+                                                (size_t)(need - copied) * cols * 8, nb, cudaMemcpyHostToDevice,
+                                                ctx->s_in));
+                copied = need;
+            }
+            FPL_CUDA(ctx, cudaMemcpyAsync(d_nmap + (size_t)a * cols * nulong, job->nmap + (size_t)a * cols * nulong,
+                                          (size_t)(b - a) * cols * nulong * 4, cudaMemcpyHostToDevice, ctx->s_in));
+            cudaEvent_t ev_in = ctx->chunk_ev[2 * c], ev_done = ctx->chunk_ev[2 * c + 1];
+            FPL_CUDA(ctx, cudaEventRecord(ev_in, ctx->s_in));
+            FPL_CUDA(ctx, cudaStreamWaitEvent(st, ev_in, 0));
+            fpl_job cj = *job;
+            cj.row_begin = a;
+            cj.row_end = b;
+            rc = fpl_enqueue(ctx, &cj, d_stack, d_nmap, d_phase, d_tcorr, d_comp, d_status, st, ctx->force_fp64,
+                             static_cast<char *>(ctx->d_small) + kCounterBlock * c, c == 0);
+            if (rc) return rc;
+            FPL_CUDA(ctx, cudaEventRecord(ev_done, st));
+            FPL_CUDA(ctx, cudaStreamWaitEvent(ctx->s_out, ev_done, 0));
+            const size_t off = (size_t)a * cols, cnt = (size_t)(b - a) * cols;
+            FPL_CUDA(ctx, cudaMemcpy2DAsync(static_cast<char *>(job->phase) + off * 8, plane * 8, d_phase + off * 8,
+                                            plane * 8, cnt * 8, nb, cudaMemcpyDeviceToHost, ctx->s_out));
+            FPL_CUDA(ctx, cudaMemcpyAsync(job->tcorr + off, d_tcorr + off, cnt * 4, cudaMemcpyDeviceToHost,
+                                          ctx->s_out));
+            FPL_CUDA(ctx, cudaMemcpyAsync(static_cast<char *>(job->comp) + off * 8, d_comp + off * 8, cnt * 8,
+                                          cudaMemcpyDeviceToHost, ctx->s_out));
+            if (job->status)
+                FPL_CUDA(ctx, cudaMemcpyAsync(job->status + off, d_status + off, cnt * 4, cudaMemcpyDeviceToHost,
+                                              ctx->s_out));
+        }
+        FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+        // the outputs and the counters are read once every chunk is done
+        FPL_CUDA(ctx, cudaStreamWaitEvent(st, ctx->chunk_ev[2 * (nchunks - 1) + 1], 0));
+        FPL_CUDA(ctx, cudaStreamSynchronize(ctx->s_out));
     }
-    FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
-    rc = fpl_enqueue(ctx, job, stack, nmap, phase, tcorr, comp, status, st, ctx->force_fp64);
-    if (rc) return rc;
-    FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
-    if (job->memory == FPL_MEM_HOST) {
-        // rows outside [row_begin,row_end) are copied back as the device
-        // buffers hold them; only the computed rows are meaningful.
-        const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
-        const size_t off = (size_t)r0 * job->cols, cnt = (size_t)(r1 - r0) * job->cols;
-        for (int b = 0; b < job->nbands; ++b)
-            FPL_CUDA(ctx, cudaMemcpyAsync(static_cast<char *>(job->phase) + (b * plane + off) * 8,
-                                          static_cast<char *>(phase) + (b * plane + off) * 8, cnt * 8,
-                                          cudaMemcpyDeviceToHost, st));
-        FPL_CUDA(ctx, cudaMemcpyAsync(job->tcorr + off, tcorr + off, cnt * 4, cudaMemcpyDeviceToHost, st));
-        FPL_CUDA(ctx, cudaMemcpyAsync(static_cast<char *>(job->comp) + off * 8, static_cast<char *>(comp) + off * 8,
-                                      cnt * 8, cudaMemcpyDeviceToHost, st));
-        if (job->status)
-            FPL_CUDA(ctx, cudaMemcpyAsync(job->status + off, status + off, cnt * 4, cudaMemcpyDeviceToHost, st));
-    }
-    int small[16];
-    FPL_CUDA(ctx, cudaMemcpyAsync(small, ctx->d_small, sizeof(small), cudaMemcpyDeviceToHost, st));
+    int small[16 * kRunChunks];
+    FPL_CUDA(ctx, cudaMemcpyAsync(small, ctx->d_small, kCounterBlock * nchunks, cudaMemcpyDeviceToHost, st));
     FPL_CUDA(ctx, cudaStreamSynchronize(st));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
-    ctx->stats.pixels = (long long)(r1 - r0) * job->cols;
-    ctx->stats.fp64_pixels = ctx->force_fp64 ? ctx->stats.pixels : small[0];
+    long long fp64 = 0, slow = 0;
+    unsigned err = 0;
+    for (int c = 0; c < nchunks; ++c) {
+        fp64 += small[16 * c];
+        err |= static_cast<unsigned>(small[16 * c + 4]);
+        slow += small[16 * c + 8];
+    }
+    ctx->stats.pixels = (long long)(r1 - r0) * cols;
+    ctx->stats.fp64_pixels = ctx->force_fp64 ? ctx->stats.pixels : fp64;
     ctx->stats.mixed_fp64_inverse = 0;
-    ctx->stats.slow_path_pixels = small[8];
+    ctx->stats.slow_path_pixels = slow;
     ctx->stats.kernel_ms = ms;
     ctx->stats.total_ms =
         std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    unsigned err = static_cast<unsigned>(small[4]);
     if (err) {
         ctx->last_error = "device error flags " + std::to_string(err);
         return FPL_ERR_DEVICE_CHECK;

@@ -9,6 +9,11 @@
 
 #include "fringe_gb300.h"
 
+// host-memory runs: row chunks whose copies overlap the compute, and the
+// 64-byte counter block of each chunk
+constexpr int kRunChunks = 8;
+constexpr size_t kCounterBlock = 64;
+
 // default tuning of the FP32 form
 constexpr float kDefaultAmbScale = 8.0f;    // FP32 rounding band, in units of n*eps*|A|_F
 constexpr float kDefaultCondMax = 1000.0f;  // |C| inverted in FP32 up to this inf-norm condition
@@ -17,7 +22,11 @@ struct fpl_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t s_in = nullptr, s_out = nullptr;   // copy streams of host-memory runs
+    std::vector<cudaEvent_t> chunk_ev;            // 2 per chunk: inputs arrived, chunk computed
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_last = nullptr;   // end of the last run enqueued on this context
+    bool last_used = false;
     // staging buffers for host-memory jobs (grown on demand)
     void *d_stack = nullptr, *d_nmap = nullptr, *d_phase = nullptr, *d_tcorr = nullptr,
          *d_comp = nullptr, *d_status = nullptr;
@@ -51,6 +60,9 @@ struct fpl_ctx {
 };
 
 int fpl_validate_job(const fpl_job *job);
+// Enqueues one run (rows [row_begin, row_end) of job) on st for device
+// buffers; counters: a kCounterBlock-byte block of device memory (NULL: the
+// context's first block); count_run: count it as a run for the profiler.
 int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
                 void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
-                bool fp64_all);
+                bool fp64_all, void *counters = nullptr, bool count_run = true);

@@ -143,8 +143,9 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job);
 
 /* Asynchronous run on `stream` (a cudaStream_t used as given: NULL is the
  * legacy default stream); device buffers only.  Runs sharing one context
- * share its scratch, so they must not overlap on the GPU.  Same replacement
- * as fpl_run. */
+ * share its scratch: each run waits on the GPU for the context's previous
+ * run, on whatever stream that was enqueued (inside a stream capture the
+ * caller's graph orders them instead).  Same replacement as fpl_run. */
 int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream);
 
 int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out);
