@@ -599,7 +599,7 @@ def main():
         "config": {"workload": "voronoi %dx%d N=%d half-window %dx%d %s evd-semantics"
                                % (R, C, NB, NY, NX, args.method),
                    "precision": args.precision, "mean_shp": sbar,
-                   "l2": "inputs (1.0 GB stack) exceed L2; no flush needed",
+                   "l2": "inputs (%.2f GB stack) exceed the 129 MB L2; no flush needed" % (stack.nbytes / 1e9),
                    "valid_px": valid, "fp64_settled_px": fp64_px},
         "e2e": e2e,
         "gpu_launches": head["launches_per_step"] * args.steps,
