@@ -168,8 +168,8 @@ def serving_measurement(njobs, seed=5):
     """Serving loop on a mix of jobs: tiles 256^2..1024^2, N in 10..60,
     half-windows 3x3..5x10, MLE/EVD, in the mixed-precision form and in the
     plain FP32 form.  Per form: (1) all jobs submitted at once (saturating
-    load): throughput and p50/p99 latency; (2) Poisson arrivals at 70% of
-    the saturated job rate: p50/p99 latency."""
+    load): throughput and p50/p99 latency; (2) Poisson arrivals at 30, 50, 70
+    and 90% of the saturated job rate: p50/p99 latency."""
     from fringe_gb300 import synth
     from fringe_gb300.serve import Server
     shapes = [(256, 10, (3, 3)), (512, 30, (5, 10)), (1024, 20, (3, 5)), (512, 60, (5, 10)),
@@ -221,16 +221,19 @@ def serving_measurement(njobs, seed=5):
         px = float(sum(pool[p][0].shape[1] * pool[p][0].shape[2] for p in picks))
         wall, lat = run(None)
         rate_sat = njobs / wall
-        rate = 0.7 * rate_sat
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs))
-        _, lat_p = run(arrivals)
+        sweep = []
+        for frac in (0.3, 0.5, 0.7, 0.9):
+            rate = frac * rate_sat
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs))
+            w, lat_p = run(arrivals)
+            sweep.append({"load": frac, "rate_jobs_per_s": rate, "throughput_px_s": px / w,
+                          "p50_ms": float(np.percentile(lat_p, 50)), "p99_ms": float(np.percentile(lat_p, 99))})
         srv.close()
         result["pixels"] = px
         result[prec] = {
             "saturated": {"throughput_px_s": px / wall, "jobs_per_s": rate_sat,
                           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
-            "poisson": {"rate_jobs_per_s": rate, "p50_ms": float(np.percentile(lat_p, 50)),
-                        "p99_ms": float(np.percentile(lat_p, 99))}}
+            "poisson": sweep}
     return result
 
 

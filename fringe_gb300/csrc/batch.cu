@@ -18,8 +18,9 @@
 // sized for one wave.  Their FP64 settle runs with the FP32 jobs' at the end.
 //
 // An optional autotuner times the candidate CTA shapes (warps per CTA) of
-// each depth class on the batch itself and keeps the fastest per
-// (NP, window taps, mean SHP count) key in the context.
+// each depth class -- the FP32 batch launches and the mixed form's solve
+// launches -- on the batch itself and keeps the fastest per (form, NP,
+// window taps, mean SHP count) key in the context.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -250,6 +251,7 @@ struct fpl_batch {
     fpl::BatchEntry *d_ments = nullptr;   // mixed: solve entries of every wave
     fpl::BatchEntry *d_m64 = nullptr;     // mixed: every piece, by padded depth (FP64 settle)
     int m64_first[3] = {0, 0, 0}, m64_count[3] = {0, 0, 0};
+    int mixed_warps[3] = {0, 0, 0};  // warps per CTA of the mixed solve launches (0: the most that fit)
     void *d_rec = nullptr;           // mixed: Gamma records and tile infos of one wave
     std::vector<BatchClass> classes;
     fpl::BatchEntry *d_table = nullptr;
@@ -288,7 +290,8 @@ int batch_enqueue(fpl_batch *b, cudaStream_t st)
                 return FPL_ERR_CUDA;
         for (int c = 0; c < 3; ++c)
             if (w.ent_count[c] && fpl::launch_solve_batch(kNP[c], b->d_ments + w.ent_first[c], w.ent_count[c],
-                                                          w.ent_total[c], ctx->num_sms, st) != cudaSuccess)
+                                                          w.ent_total[c], ctx->num_sms, st,
+                                                          b->mixed_warps[c]) != cudaSuccess)
                 return FPL_ERR_CUDA;
     }
     for (const BatchClass &k : b->classes)
@@ -577,6 +580,54 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
                 if (ms < best) { best = ms; best_w = w; }
             }
             k.warps = best_w;
+            ctx->tuned_warps[key] = best_w;
+        }
+        // mixed form: warps per CTA of the solve launches of each padded depth,
+        // keyed like the FP32 classes with a bit for the form
+        for (int c = 0; c < 3; ++c) {
+            if (!b->m64_count[c]) continue;
+            const int np = 16 << c;
+            unsigned long long shp = 0, px = 0;
+            int taps = 0;
+            std::vector<fpl::BatchEntry> pcs(b->m64_count[c]);
+            cudaMemcpy(pcs.data(), b->d_m64 + b->m64_first[c], sizeof(fpl::BatchEntry) * pcs.size(),
+                       cudaMemcpyDeviceToHost);
+            for (const fpl::BatchEntry &en : pcs) {
+                const fpl::KParams &P = en.P;
+                taps = std::max(taps, P.K);
+                cudaMemsetAsync(d_sum, 0, sizeof(unsigned long long), b->cap_stream);
+                fpl::k_popcount<<<256, 256, 0, b->cap_stream>>>(P.nmap + P.pix_begin * P.nulong,
+                                                                 P.npix * P.nulong, d_sum);
+                unsigned long long sum = 0;
+                cudaMemcpyAsync(&sum, d_sum, sizeof(sum), cudaMemcpyDeviceToHost, b->cap_stream);
+                cudaStreamSynchronize(b->cap_stream);
+                shp += sum;
+                px += (unsigned long long)P.npix;
+            }
+            const long long key = (1ll << 62) | ((long long)np << 40) | ((long long)taps << 16) |
+                                  (long long)(px ? shp / px / 16 : 0);
+            auto it = ctx->tuned_warps.find(key);
+            if (it != ctx->tuned_warps.end()) {
+                b->mixed_warps[c] = it->second;
+                continue;
+            }
+            const int wmax = fpl::solve_max_warps(np);
+            const int cands[3] = {std::max(1, wmax / 2), std::max(1, (3 * wmax) / 4), wmax};
+            float best = 1e30f;
+            int best_w = wmax;
+            for (int ci = 0; ci < 3; ++ci) {
+                const int w = cands[ci];
+                if (ci > 0 && w == cands[ci - 1]) continue;
+                b->mixed_warps[c] = w;
+                cudaEventRecord(e0, b->cap_stream);
+                if (batch_enqueue(b, b->cap_stream) != FPL_OK) break;
+                cudaEventRecord(e1, b->cap_stream);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) { best = ms; best_w = w; }
+            }
+            b->mixed_warps[c] = best_w;
             ctx->tuned_warps[key] = best_w;
         }
         cudaEventDestroy(e0);

@@ -48,8 +48,10 @@ cudaError_t launch_gram_batch(int kc, const BoxSeg *segs, int nseg, long long to
 // before capturing a launch sequence)
 cudaError_t prepare_mixed_batch(int np);
 cudaError_t prepare_gram_batch();
-// eigen-solves of every entry (one padded depth np) in one persistent launch
+// eigen-solves of every entry (one padded depth np) in one persistent launch;
+// warps: warps per CTA (0 = the most that fit; see solve_max_warps)
 cudaError_t launch_solve_batch(int np, const BatchEntry *ents, int nent, long long total, int num_sms,
-                               cudaStream_t st);
+                               cudaStream_t st, int warps = 0);
+int solve_max_warps(int np);
 
 }  // namespace fpl

@@ -1,4 +1,6 @@
 // kernels_f32.cu -- FP32 instantiations of the pixel kernels.
+#include <algorithm>
+
 #include "kernels_impl.cuh"
 
 namespace fpl {
@@ -43,14 +45,24 @@ cudaError_t prepare_mixed_batch(int np)
     return cudaErrorInvalidValue;
 }
 
+int solve_max_warps(int np)
+{
+    switch (np) {
+    case 16: return std::min(32, int((224 * 1024) / Lay<float, 16>::bytes_noc));
+    case 32: return std::min(32, int((224 * 1024) / Lay<float, 32>::bytes_noc));
+    case 64: return std::min(16, int((224 * 1024) / Lay<float, 64>::bytes));
+    }
+    return 1;
+}
+
 cudaError_t launch_solve_batch(int np, const BatchEntry *ents, int nent, long long total, int num_sms,
-                               cudaStream_t st)
+                               cudaStream_t st, int warps)
 {
     if (nent <= 0 || total <= 0) return cudaSuccess;
     switch (np) {
-    case 16: return launch_solve_batch_t<16, true>(ents, nent, total, num_sms, st);
-    case 32: return launch_solve_batch_t<32, true>(ents, nent, total, num_sms, st);
-    case 64: return launch_solve_batch_t<64, false>(ents, nent, total, num_sms, st);
+    case 16: return launch_solve_batch_t<16, true>(ents, nent, total, num_sms, st, warps);
+    case 32: return launch_solve_batch_t<32, true>(ents, nent, total, num_sms, st, warps);
+    case 64: return launch_solve_batch_t<64, false>(ents, nent, total, num_sms, st, warps);
     }
     return cudaErrorInvalidValue;
 }

@@ -136,13 +136,14 @@ __global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve_batch(const BatchEn
 // CTA shape of the solve kernels: warps per CTA by shared memory (and
 // registers), one CTA per SM in the tensor-memory form
 template <int NP, bool TM, typename K>
-static cudaError_t solve_shape(K kern, int *warps_out, int *per_sm_out, size_t *smem_out)
+static cudaError_t solve_shape(K kern, int *warps_out, int *per_sm_out, size_t *smem_out, int warps_req = 0)
 {
     const size_t per_warp = TM ? Lay<float, NP>::bytes_noc : Lay<float, NP>::bytes;
     const size_t budget = 224 * 1024;
     const int cap = TM ? 32 : 16;
     int warps = int(budget / per_warp);
     if (warps > cap) warps = cap;
+    if (warps_req > 0 && warps > warps_req) warps = warps_req;
     if (warps < 1) warps = 1;
     int per_sm = 0;
     size_t smem = per_warp * warps;
@@ -202,15 +203,17 @@ static cudaError_t configure_solve_batch()
     return solve_configure(k_solve_batch<NP, TM>, configured);
 }
 
+// warps_req > 0: at most that many warps per CTA (the batch autotuner's
+// candidates); 0: as many as shared memory and registers allow
 template <int NP, bool TM>
 static cudaError_t launch_solve_batch_t(const BatchEntry *ents, int nent, long long total, int num_sms,
-                                       cudaStream_t st)
+                                       cudaStream_t st, int warps_req)
 {
     cudaError_t e = configure_solve_batch<NP, TM>();
     if (e != cudaSuccess) return e;
     int warps = 0, per_sm = 0;
     size_t smem = 0;
-    if ((e = solve_shape<NP, TM>(k_solve_batch<NP, TM>, &warps, &per_sm, &smem)) != cudaSuccess) return e;
+    if ((e = solve_shape<NP, TM>(k_solve_batch<NP, TM>, &warps, &per_sm, &smem, warps_req)) != cudaSuccess) return e;
     long long blocks = (long long)num_sms * per_sm;
     long long need = (total + warps - 1) / warps;
     if (need < blocks) blocks = need > 0 ? need : 1;

@@ -159,8 +159,11 @@ int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out);
  * loop).  FPL_BATCH_GRAPH captures the launch sequence into a CUDA graph at
  * creation; fpl_batch_run replays it (buffers are fixed, their contents may
  * change between runs).  FPL_BATCH_AUTOTUNE times candidate CTA shapes on
- * the batch at creation and caches the fastest per (depth, window, mean SHP
- * count) in the context.  Batches use the plain FP32 form. */
+ * the batch at creation and caches the fastest per (form, depth, window,
+ * mean SHP count) in the context.  Jobs with precision FPL_PREC_MIXED run
+ * the mixed form: cut into row pieces, packed into waves of <= 2^20 pixels,
+ * one tensor-core Gamma launch over the tiles and one solve launch over the
+ * pixels of each wave. */
 #define FPL_BATCH_GRAPH 1
 #define FPL_BATCH_AUTOTUNE 2
 typedef struct fpl_batch fpl_batch;

@@ -30,7 +30,7 @@ def _jobs(torch):
 
 @pytest.mark.parametrize("graph,autotune,precision", [
     (True, False, "fp32"), (False, False, "fp32"), (True, True, "fp32"),
-    (True, False, "mixed"), (False, False, "mixed"), (True, False, "both")])
+    (True, False, "mixed"), (False, False, "mixed"), (True, True, "mixed"), (True, False, "both")])
 def test_batch_equals_single_jobs(gpu_lib, graph, autotune, precision):
     torch = pytest.importorskip("torch")
     from fringe_gb300.linker import PhaseLinkBatch, phase_link
