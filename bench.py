@@ -50,6 +50,15 @@ SEED = 1002
 METRIC = "phase-linked px/s (N=30, 11x21)"
 
 
+# what the ncu captures under profiles/ show for each kernel
+BOUND_NOTES = {
+    "solve": "instruction issue: 64% issue-active at 20 warps/SM, 26.2k warp instructions per pixel "
+             "(per-pixel FP32 factorisations and triangular solves); DRAM 1.5%, tensor pipe 0%",
+    "gram": "operand build on the CUDA cores with 8 warps/SM: tensor pipe 17.5% active, issue 35%",
+    "fp32": "per-pixel FP32 gather, Gamma and eigen-solves: latency/issue-bound with 8-11 warps/SM",
+}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -613,7 +622,8 @@ def main():
                      "work": "Gamma flops 4N(N+1)S summed over pixels, per step",
                      "kernel_ms": k_ms,
                      "hbm_achieved_gbs": alg_bytes / (k_ms / 1e3) / 1e9,
-                     "hbm_peak_gbs": hbm_peak},
+                     "hbm_peak_gbs": hbm_peak,
+                     "what_bounds_it": BOUND_NOTES.get(dom, "")},
         "kernels": per_kernel,
     }
     if not args.no_compare:

@@ -6,7 +6,9 @@
 // service that must not allocate after start-up.  Such a caller passes its
 // own input and output buffers, and the kernels' scratch -- the list of
 // pixels settled by the FP64 pass and its counters -- lives in the
-// file-scope array below instead of context buffers.
+// file-scope array below instead of context buffers.  It runs the plain FP32
+// form whatever the job's precision: the mixed form's coherence records
+// (3.8 KB per pixel at 30 dates) are far beyond a fixed array.
 //
 // The array is a fixed-size __device__ variable: every GPU that loads this
 // library holds its 4 MiB (plus 256 bytes) until the process exits.  Its

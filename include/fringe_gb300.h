@@ -205,8 +205,10 @@ int fpl_server_destroy(fpl_server *srv);
 /* ---- run without device allocation (no counterpart in the reference) -----
  * For callers that cannot call cudaMalloc -- an application whose device
  * memory belongs to another allocator, or a service that must not allocate
- * after start-up.  Same job and results as fpl_run_async on device buffers,
- * on the current CUDA device, but no context is needed and nothing is
+ * after start-up.  Same job and results as fpl_run_async on device buffers
+ * in the plain FP32 form (a job asking for the mixed form runs the FP32 form
+ * here: the mixed form's coherence records need gigabytes of scratch), on
+ * the current CUDA device, but no context is needed and nothing is
  * allocated: the kernels' scratch is a fixed array inside the library, held
  * by every GPU that loads it until the process exits.  The first call on a
  * device looks up that array's device address; make that first call before

@@ -152,3 +152,34 @@ def test_golden_vectors_from_the_reference(gpu_lib):
             m = compare(got, ref)
             assert m["valid_both"] > 0, (case, var, m)
             assert_parity(m)
+
+
+def test_scene_past_32_bit_indices(gpu_lib):
+    """A 8448 x 8704 scene of 30 dates (N * pixels > 2^31) tiled on the device
+    from a seeded 256 x 256 block: pixels whose windows lie inside one copy
+    equal the block's own results bit for bit (mixed form over the whole
+    scene, plain FP32 form over its last rows)."""
+    torch = pytest.importorskip("torch")
+    from fringe_gb300 import phase_link
+    B, N, ny, nx = 256, 30, 5, 10
+    stack, nmap = synth.scene("voronoi", B, B, N, ny, nx, seed=808)
+    ref_mixed = phase_link(stack, nmap, (ny, nx), precision="mixed")
+    ref_fp32 = phase_link(stack, nmap, (ny, nx), precision="fp32")
+    TR, TC = 33, 34
+    d_stack = torch.from_numpy(stack).cuda().repeat(1, TR, TC)
+    d_nmap = torch.from_numpy(nmap.view(np.int32)).cuda().repeat(TR, TC, 1)
+    R, C = B * TR, B * TC
+    assert N * R * C > 2 ** 31
+    inner = (slice(ny, B - ny), slice(nx, B - nx))
+    out = phase_link(d_stack, d_nmap, (ny, nx), precision="mixed")
+    for tr, tc in ((0, 0), (TR - 1, TC - 1), (17, 5)):
+        sl = (slice(tr * B, (tr + 1) * B), slice(tc * B, (tc + 1) * B))
+        t = out["tcorr"][sl].cpu().numpy()[inner]
+        assert np.array_equal(t, ref_mixed["tcorr"][inner], equal_nan=True), (tr, tc)
+        p = out["phase"][:, sl[0], sl[1]].cpu().numpy()[:, inner[0], inner[1]]
+        assert np.array_equal(p, ref_mixed["phase"][:, inner[0], inner[1]]), (tr, tc)
+    del out
+    r0 = (TR - 1) * B
+    out = phase_link(d_stack, d_nmap, (ny, nx), precision="fp32", rows=(r0, R))
+    t = out["tcorr"][r0:, (TC - 1) * B:].cpu().numpy()[inner]
+    assert np.array_equal(t, ref_fp32["tcorr"][inner], equal_nan=True)
