@@ -28,7 +28,7 @@ cudaError_t launch_solve(const KParams &P, int num_sms, cudaStream_t st)
     switch (pick_np(P.nb)) {
     case 16: return launch_solve_t<16, true>(P, num_sms, st);
     case 32: return launch_solve_t<32, true>(P, num_sms, st);
-    case 64: return launch_solve_t<64, false>(P, num_sms, st);
+    case 64: return launch_solve_t<64, true>(P, num_sms, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -40,7 +40,7 @@ cudaError_t prepare_mixed_batch(int np)
     switch (np) {
     case 16: return configure_solve_batch<16, true>();
     case 32: return configure_solve_batch<32, true>();
-    case 64: return configure_solve_batch<64, false>();
+    case 64: return configure_solve_batch<64, true>();
     }
     return cudaErrorInvalidValue;
 }
@@ -50,7 +50,7 @@ int solve_max_warps(int np)
     switch (np) {
     case 16: return std::min(32, int((224 * 1024) / Lay<float, 16>::bytes_noc));
     case 32: return std::min(32, int((224 * 1024) / Lay<float, 32>::bytes_noc));
-    case 64: return std::min(16, int((224 * 1024) / Lay<float, 64>::bytes));
+    case 64: return std::min(8, int((224 * 1024) / Lay<float, 64>::bytes_noc));
     }
     return 1;
 }
@@ -62,7 +62,7 @@ cudaError_t launch_solve_batch(int np, const BatchEntry *ents, int nent, long lo
     switch (np) {
     case 16: return launch_solve_batch_t<16, true>(ents, nent, total, num_sms, st, warps);
     case 32: return launch_solve_batch_t<32, true>(ents, nent, total, num_sms, st, warps);
-    case 64: return launch_solve_batch_t<64, false>(ents, nent, total, num_sms, st, warps);
+    case 64: return launch_solve_batch_t<64, true>(ents, nent, total, num_sms, st, warps);
     }
     return cudaErrorInvalidValue;
 }

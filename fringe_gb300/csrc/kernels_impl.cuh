@@ -9,6 +9,7 @@
 // Both are persistent: the grid is sized to the resident capacity of the
 // GPU and warps stride over their pixels.
 #pragma once
+#include <type_traits>
 #include "kernels.h"
 #include "pixel.cuh"
 
@@ -38,7 +39,7 @@ __global__ void k_pixels(KParams P)
 // about twice as many warps; the kernel issues no MMA.
 __device__ __forceinline__ int tmem_cols_for(int warps, int np)
 {
-    int need = ((warps + 3) / 4) * 2 * np, cols = 32;
+    int need = ((warps + 3) / 4) * 2 * np * ((np + 31) / 32), cols = 32;
     while (cols < need) cols <<= 1;
     return cols;
 }
@@ -52,6 +53,13 @@ __device__ __forceinline__ void solve_pixel(const KParams &P, long long pp, unsi
         const int npix = pixel_load_gamma<NP, false>(P, pp, sm, lane, A);
         if (npix >= 0 && rows_coherence<NP>(P, pp, A, sm, cp, lane))
             pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
+    } else if constexpr (std::is_same<CP, CRowsTmem<NP>>::value) {
+        // two rows per lane: normalise in the slab, then copy the rows over
+        const int npix = pixel_load_gamma<NP>(P, pp, sm, lane, A);
+        if (npix >= 0) {
+            rows_from_smem<NP>(cp, A, lane);
+            pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
+        }
     } else {
         const int npix = pixel_load_gamma<NP>(P, pp, sm, lane, A);
         if (npix >= 0) pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
@@ -84,7 +92,8 @@ __device__ __forceinline__ void solve_loop(long long total, const SRC &src)
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t tbase = tslot;
-        const CRowsTmem<NP> cp{tbase + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * 2 * NP)};
+        const CRowsTmem<NP> cp{tbase + ((uint32_t)(32 * (warp & 3)) << 16) +
+                               (uint32_t)(warp >> 2) * CRowsTmem<NP>::kColsPerWarp};
         C2<float> *A = reinterpret_cast<C2<float> *>(sm + Lay<float, NP>::wm);
         for (long long q = gw; q < total; q += nw) {
             long long pp;
@@ -109,7 +118,7 @@ __device__ __forceinline__ void solve_loop(long long total, const SRC &src)
 }
 
 template <int NP, bool TM>
-__global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve(KParams P)
+__global__ void __launch_bounds__((TM && NP <= 32) ? 640 : (TM ? 256 : 512), 1) k_solve(KParams P)
 {
     solve_loop<NP, TM>(P.npix, [&](long long q, long long &pp) -> const KParams & {
         pp = P.pix_begin + q;
@@ -119,7 +128,7 @@ __global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve(KParams P)
 
 // the mixed form over many launches of one padded depth
 template <int NP, bool TM>
-__global__ void __launch_bounds__(TM ? 640 : 512, 1) k_solve_batch(const BatchEntry *__restrict__ ents, int nent,
+__global__ void __launch_bounds__((TM && NP <= 32) ? 640 : (TM ? 256 : 512), 1) k_solve_batch(const BatchEntry *__restrict__ ents, int nent,
                                                                   long long total)
 {
     solve_loop<NP, TM>(total, [&](long long q, long long &pp) -> const KParams & {
@@ -140,7 +149,8 @@ static cudaError_t solve_shape(K kern, int *warps_out, int *per_sm_out, size_t *
 {
     const size_t per_warp = TM ? Lay<float, NP>::bytes_noc : Lay<float, NP>::bytes;
     const size_t budget = 224 * 1024;
-    const int cap = TM ? 32 : 16;
+    // tensor memory: 512 columns per lane quadrant, CRowsTmem<NP>::kColsPerWarp per warp
+    const int cap = TM ? int(4 * (512 / CRowsTmem<NP>::kColsPerWarp)) : 16;
     int warps = int(budget / per_warp);
     if (warps > cap) warps = cap;
     if (warps_req > 0 && warps > warps_req) warps = warps_req;

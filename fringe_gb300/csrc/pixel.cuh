@@ -199,8 +199,9 @@ template <typename T, int NP> struct CRowsSmem {
     __device__ __forceinline__ void fence() const { __syncwarp(); }
 };
 
-// C in tensor memory (FP32, NP <= 32): the warp owns 2*NP 32-bit columns
-// of its 32 TMEM lanes; lane l holds row l (Re, Im interleaved).  The solver
+// C in tensor memory (FP32, NP <= 64): the warp owns 2*NP 32-bit columns
+// of its 32 TMEM lanes per row slot; lane l holds row l (and row l + 32 in a
+// second block of 2*NP columns when NP = 64), Re and Im interleaved.  The solver
 // kernels issue no MMA: tensor memory is extra per-warp storage there,
 // which frees shared memory for more resident warps.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
@@ -225,12 +226,14 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16
 }
 
 template <int NP> struct CRowsTmem {
-    static_assert(NP <= 32, "one row per lane");
+    static_assert(NP <= 64, "at most two rows per lane");
+    // row slot h of the lane (row lane + 32 h) starts 2*NP columns after slot h-1
+    static constexpr uint32_t kColsPerWarp = 2u * NP * ((NP + 31) / 32);
     uint32_t taddr;      // lane quadrant << 16 | first column of the warp
     __device__ __forceinline__ void load(int h, int c, C2<float> (&v)[8]) const
     {
         uint32_t r[16];
-        tmem_ld16(taddr + 16u * (uint32_t)c, r);
+        tmem_ld16(taddr + (uint32_t)(2 * NP * h) + 16u * (uint32_t)c, r);
 #pragma unroll
         for (int k = 0; k < 8; ++k) v[k] = cmk<float>(__uint_as_float(r[2 * k]), __uint_as_float(r[2 * k + 1]));
     }
@@ -242,7 +245,7 @@ template <int NP> struct CRowsTmem {
             r[2 * k] = __float_as_uint(v[k].x);
             r[2 * k + 1] = __float_as_uint(v[k].y);
         }
-        tmem_st16(taddr + 16u * (uint32_t)c, r);
+        tmem_st16(taddr + (uint32_t)(2 * NP * h) + 16u * (uint32_t)c, r);
     }
     __device__ __forceinline__ void fence() const
     {
@@ -1772,6 +1775,26 @@ __device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *s
     __syncwarp();
     if (!NORMALIZE) return info;
     return gamma_to_coherence<float, NP>(P, pp, Cm, sm, lane) ? info : -1;
+}
+
+// rows of the coherence matrix C in shared memory (ld NP+1, full storage)
+// into the row policy cp (every lane calls it together)
+template <int NP, typename CP>
+__device__ void rows_from_smem(const CP &cp, const C2<float> *A, int lane)
+{
+#pragma unroll
+    for (int h = 0; h < RowShape<NP>::H; ++h) {
+        const int i = lane + 32 * h;
+#pragma unroll 1
+        for (int c = 0; c < RowShape<NP>::CH; ++c) {
+            C2<float> v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = (i < NP) ? A[i * (NP + 1) + 8 * c + k] : cmk<float>(0.f, 0.f);
+            cp.store(h, c, v);
+        }
+    }
+    cp.fence();
+    __syncwarp();
 }
 
 // Gamma (upper triangle and diagonal of G, ld NP+1) to coherence rows in
