@@ -447,37 +447,64 @@ __device__ __forceinline__ bool warp_chol_any(C2<T> *A, int n, C2<T> *col, int l
         return warp_chol_c<T, LD, NP, STORE>(A, n, col, lane);
 }
 
-// Solves (L L^H) x = b with the factor of warp_chol_c<STORE> (1/L_jj on the
-// diagonal).  b / x are lane-distributed (element i on lane i%32, slot i/32).
+// Turns the factor of warp_chol_c<STORE> (L below the diagonal, 1/L_jj on
+// it, anything above it) into the strict-lower form of warp_chol_solve:
+// zeros on and above the diagonal, 1/L_ii returned per lane (d0: row lane,
+// d1: row lane + 32).
 template <typename T, int LD, int NP>
-__device__ void warp_chol_solve(const C2<T> *L, int n, C2<T> &b0, C2<T> &b1, int lane)
+__device__ void chol_strict_lower(C2<T> *L, int n, T &d0, T &d1, int lane)
 {
-    const int i0 = lane, i1 = lane + 32;
+#pragma unroll
+    for (int h = 0; h < (NP + 31) / 32; ++h) {
+        const int i = lane + 32 * h;
+        T d = T(0);
+        if (i < n) {
+            C2<T> *Li = L + i * LD;
+            d = Li[i].x;
+            for (int k = i; k < n; ++k) Li[k] = cmk<T>(T(0), T(0));
+        }
+        if (h == 0) d0 = d;
+        else d1 = d;
+    }
+    __syncwarp();
+}
+
+// Solves (L L^H) x = b for a factor in strict-lower form (see
+// chol_strict_lower).  b / x are lane-distributed (element i on lane i%32,
+// slot i/32).  Because L_ij = 0 for j >= i, every lane takes every update
+// unpredicated: step j broadcasts b_j / L_jj from lane j (final after step
+// j-1) and each row subtracts its multiple, so a step is two multiplies,
+// two shuffles, one shared load and four fused multiply-adds.  Rows at or
+// beyond n come back zero.
+template <typename T, int LD, int NP>
+__device__ void warp_chol_solve(const C2<T> *L, int n, T d0, T d1, C2<T> &b0, C2<T> &b1, int lane)
+{
+    const C2<T> *L0 = L + lane * LD;
+    const C2<T> *L1 = L + (lane + 32) * LD;
     // forward: L y = b
+#pragma unroll 4
     for (int j = 0; j < n; ++j) {
-        const C2<T> own = (j < 32) ? b0 : b1;
+        C2<T> s = (NP <= 32 || j < 32) ? cscale(b0, d0) : cscale(b1, d1);
         C2<T> y;
-        y.x = __shfl_sync(0xffffffffu, own.x, j & 31);
-        y.y = __shfl_sync(0xffffffffu, own.y, j & 31);
-        y = cscale(y, L[j * LD + j].x);
-        if (i0 == j) b0 = y;
-        if (NP > 32 && i1 == j) b1 = y;
-        if (i0 > j && i0 < n) fms_mul(b0, L[i0 * LD + j], y);
-        if (NP > 32 && i1 > j && i1 < n) fms_mul(b1, L[i1 * LD + j], y);
+        y.x = __shfl_sync(0xffffffffu, s.x, j & 31);
+        y.y = __shfl_sync(0xffffffffu, s.y, j & 31);
+        fms_mul(b0, L0[j], y);
+        if (NP > 32) fms_mul(b1, L1[j], y);
     }
-    // backward: L^H x = y
+    b0 = cscale(b0, d0);
+    if (NP > 32) b1 = cscale(b1, d1);
+    // backward: L^H x = y, b_i -= conj(L_ji) x_j
+#pragma unroll 4
     for (int j = n - 1; j >= 0; --j) {
-        const C2<T> own = (j < 32) ? b0 : b1;
+        C2<T> s = (NP <= 32 || j < 32) ? cscale(b0, d0) : cscale(b1, d1);
         C2<T> x;
-        x.x = __shfl_sync(0xffffffffu, own.x, j & 31);
-        x.y = __shfl_sync(0xffffffffu, own.y, j & 31);
-        x = cscale(x, L[j * LD + j].x);
-        if (i0 == j) b0 = x;
-        if (NP > 32 && i1 == j) b1 = x;
-        // b_i -= conj(L_ji) x_j for i < j
-        if (i0 < j) fms_cmul(b0, L[j * LD + i0], x);
-        if (NP > 32 && i1 < j) fms_cmul(b1, L[j * LD + i1], x);
+        x.x = __shfl_sync(0xffffffffu, s.x, j & 31);
+        x.y = __shfl_sync(0xffffffffu, s.y, j & 31);
+        fms_cmul(b0, L[j * LD + lane], x);
+        if (NP > 32) fms_cmul(b1, L[j * LD + lane + 32], x);
     }
+    b0 = (lane < n) ? cscale(b0, d0) : cmk<T>(T(0), T(0));
+    if (NP > 32) b1 = (lane + 32 < n) ? cscale(b1, d1) : cmk<T>(T(0), T(0));
 }
 
 // lambda_min(A) vs thr for a complex Hermitian A (lower triangle read):
@@ -588,41 +615,42 @@ __device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf
     float x[NP];
 #pragma unroll
     for (int j = 0; j < NP; ++j) x[j] = (lane < n && j < n) ? A[lane * LD + j] : 0.f;
-    for (int k = 0; k < n; ++k) {
-        float *rk = rowb + (k & 1) * NP;
-        if (lane == k) {
+    // k = 8 kb + ku with ku unrolled, so column k's register is one of
+    // NP / 8 candidates
+    for (int kb = 0; kb < NP / 8; ++kb) {
+        if (8 * kb >= n) break;
 #pragma unroll
-            for (int j = 0; j < NP; j += 4) *reinterpret_cast<float4 *>(rk + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
-        }
-        __syncwarp();
-        const float p = rk[k];
-        if (!(p > 0.f)) return false;
-        const float rp = 1.f / p;
-        const bool own = (lane == k);
-        // row k: a_kj / p;  other rows: a_ij - (a_ik / p) a_kj  (a_ik = a_ki).
-        // Lane k published its own row (r = x), so one fused multiply-add
-        // serves both: x + (1/p - 1) x on lane k, x - f r elsewhere.
-        const float f = ((lane < NP) ? rk[lane] : 0.f) * rp;
-        const float bm = own ? rp - 1.f : -f;
+        for (int ku = 0; ku < 8; ++ku) {
+            const int k = 8 * kb + ku;
+            if (k >= n) break;
+            float *rk = rowb + (ku & 1) * NP;
+            if (lane == k) {
 #pragma unroll
-        for (int j = 0; j < NP; j += 4) {
-            const float4 r = *reinterpret_cast<const float4 *>(rk + j);
-            x[j] = fmaf(bm, r.x, x[j]);
-            x[j + 1] = fmaf(bm, r.y, x[j + 1]);
-            x[j + 2] = fmaf(bm, r.z, x[j + 2]);
-            x[j + 3] = fmaf(bm, r.w, x[j + 3]);
-        }
-        // column k: x[k] = own ? -1/p : a_ik / p (k is a loop variable, so
-        // the register is chosen by block of 8)
-        const float vk = own ? -rp : f;
-        const int kb = k >> 3, ku = k & 7;
-#pragma unroll
-        for (int b = 0; b < NP / 8; ++b) {
-            if (kb == b) {
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (ku == u) x[8 * b + u] = vk;
+                for (int j = 0; j < NP; j += 4) *reinterpret_cast<float4 *>(rk + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
             }
+            __syncwarp();
+            const float p = rk[k];
+            if (!(p > 0.f)) return false;
+            const float rp = 1.f / p;
+            const bool own = (lane == k);
+            // row k: a_kj / p;  other rows: a_ij - (a_ik / p) a_kj  (a_ik = a_ki).
+            // Lane k published its own row (r = x), so one fused multiply-add
+            // serves both: x + (1/p - 1) x on lane k, x - f r elsewhere.
+            const float f = ((lane < NP) ? rk[lane] : 0.f) * rp;
+            const float bm = own ? rp - 1.f : -f;
+#pragma unroll
+            for (int j = 0; j < NP; j += 4) {
+                const float4 r = *reinterpret_cast<const float4 *>(rk + j);
+                x[j] = fmaf(bm, r.x, x[j]);
+                x[j + 1] = fmaf(bm, r.y, x[j + 1]);
+                x[j + 2] = fmaf(bm, r.z, x[j + 2]);
+                x[j + 3] = fmaf(bm, r.w, x[j + 3]);
+            }
+            // column k: x[k] = own ? -1/p : a_ik / p
+            const float vk = own ? -rp : f;
+#pragma unroll
+            for (int b = 0; b < NP / 8; ++b)
+                if (kb == b) x[8 * b + ku] = vk;
         }
     }
     __syncwarp();
@@ -1038,11 +1066,13 @@ __device__ int warp_inverse_iteration(C2<T> *W, int n, T sigma, unsigned char *s
     for (int i = lane; i < n; i += 32) W[i * LD + i].x -= sigma;
     __syncwarp();
     if (!warp_chol_any<T, LD, NP, true>(W, n, col, lane)) return -1;
+    T d0 = T(0), d1 = T(0);
+    chol_strict_lower<T, LD, NP>(W, n, d0, d1, lane);
     const T tol = (sizeof(T) == 4) ? T(1e-5) : T(1e-12);
     T rprev = T(-1), cprev = T(1), gap_good = T(0);
     for (int it = 0; it < 10; ++it) {
         C2<T> x0 = z0, x1 = z1;
-        warp_chol_solve<T, LD, NP>(W, n, x0, x1, lane);
+        warp_chol_solve<T, LD, NP>(W, n, d0, d1, x0, x1, lane);
         const T xx = warp_sum(cabs2(x0) + cabs2(x1));
         const T xv = warp_sum(ccmul(x0, z0).x + ccmul(x1, z1).x);
         const T rho = sigma + xv / xx;
