@@ -98,6 +98,11 @@ __device__ __forceinline__ void solve_loop(long long total, const SRC &src)
         for (long long q = gw; q < total; q += nw) {
             long long pp;
             const KParams &P = src(q, pp);
+            if (q + nw < total) {
+                long long pn;
+                const KParams &Pn = src(q + nw, pn);
+                prefetch_record(Pn, pn, lane);
+            }
             solve_pixel<NP>(P, pp, sm, lane, cp, A);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -112,6 +117,11 @@ __device__ __forceinline__ void solve_loop(long long total, const SRC &src)
         for (long long q = gw; q < total; q += nw) {
             long long pp;
             const KParams &P = src(q, pp);
+            if (q + nw < total) {
+                long long pn;
+                const KParams &Pn = src(q + nw, pn);
+                prefetch_record(Pn, pn, lane);
+            }
             solve_pixel<NP>(P, pp, sm, lane, cp, Cm);
         }
     }

@@ -1725,7 +1725,10 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             const int i = lane + 32 * h;
             const int ulim = (i < n) ? (stbas ? min(i + P.bw + 1, n) : n) : 0;
             const float2 pi = (i < n) ? phs[i] : make_float2(0.f, 0.f);
-            const C2<T> cpi = cmk<T>(T(pi.x), T(pi.y));
+            cnt += max(ulim - i - 1, 0);
+            // sum_j exp(i arg C_ij) ph_j over the row, then times conj(ph_i):
+            // exp(i(arg C_ij - arg ph_i + arg ph_j)) summed over j > i
+            T wr = T(0), wi = T(0);
 #pragma unroll 1
             for (int cc = 0; cc < RS::CH; ++cc) {
                 C2<T> cv[8];
@@ -1738,13 +1741,14 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
                     const T ca2 = cabs2(c);
                     const C2<T> u = (ca2 > T(0)) ? cscale(c, rsqrt_t(ca2)) : cmk<T>(T(1), T(0));
                     const float2 pj = phs[j];
-                    // exp(i(arg C_ij - arg ph_i + arg ph_j))
-                    const C2<T> v = cmul(cmulc(u, cpi), cmk<T>(T(pj.x), T(pj.y)));
-                    sr += v.x;
-                    si += v.y;
-                    cnt++;
+                    const C2<T> v = cmul(u, cmk<T>(T(pj.x), T(pj.y)));
+                    wr += v.x;
+                    wi += v.y;
                 }
             }
+            const C2<T> w = cmulc(cmk<T>(wr, wi), cmk<T>(T(pi.x), T(pi.y)));
+            sr += w.x;
+            si += w.y;
         }
         sr = warp_sum(sr);
         si = warp_sum(si);
@@ -1756,6 +1760,20 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
     }
 }
 
+
+// Mixed form: pulls the Gamma record and tile information of pixel pp of P
+// into L2 (one 128-byte line per lane), so the load of the next pixel of a
+// warp finds them there.
+__device__ __forceinline__ void prefetch_record(const KParams &P, long long pp, int lane)
+{
+    const long long loc = pp - P.cbase;
+    const char *rec = reinterpret_cast<const char *>(P.cbuf) + loc * (long long)P.cstride * 4;
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(rec) & ~uintptr_t(127);
+    const uintptr_t hi = reinterpret_cast<uintptr_t>(rec) + (size_t)P.cstride * 4;
+    for (uintptr_t a = lo + 128u * (unsigned)lane; a < hi; a += 32u * 128u)
+        asm volatile("prefetch.L2 [%0];" :: "l"(a));
+    if (lane == 31) asm volatile("prefetch.L2 [%0];" :: "l"(P.cinfo + loc));
+}
 
 // Mixed form: Gamma of pixel pp was accumulated on the tensor cores
 // (gram_box.cu) into a record of P.cstride floats; load it into the shared-
@@ -1786,21 +1804,38 @@ __device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *s
         defer_fp64(P, pp, lane);
         return -1;
     }
-    const float *rec = reinterpret_cast<const float *>(P.cbuf) + loc * (long long)P.cstride;
+    const float4 *rec4 =
+        reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(P.cbuf) + loc * (long long)P.cstride);
     const int dp = (n + 1) >> 1, nblk = dp * (dp + 1) / 2;
-    // blocks t = 0 .. nblk-1, row-major over the upper triangle of pairs:
-    // pair row a holds blocks (a, a) .. (a, dp-1)
-    for (int t = lane; t < nblk; t += 32) {
-        int a = 0, rem = t;
-        while (rem >= dp - a) { rem -= dp - a; ++a; }
-        const int b = a + rem;
-        const float4 *blk = reinterpret_cast<const float4 *>(rec + 8 * t);
-        const float4 u = __ldg(blk), v = __ldg(blk + 1);
-        const int i0 = 2 * a, i1 = 2 * a + 1, j0 = 2 * b, j1 = 2 * b + 1;
-        if (j0 < n) Cm[i0 * LD + j0] = cmk<float>(u.x, u.y);
-        if (j1 < n) Cm[i0 * LD + j1] = cmk<float>(u.z, u.w);
-        if (i1 < n && j0 >= i1) Cm[i1 * LD + j0] = cmk<float>(v.x, v.y);
-        if (j1 < n) Cm[i1 * LD + j1] = cmk<float>(v.z, v.w);
+    // blocks t = 0 .. nblk-1, row-major over the upper triangle of pairs
+    // (pair row a holds blocks (a, a) .. (a, dp-1)).  Counted from the last
+    // block, t' = nblk-1-t lies in pair row a = dp-1-r for r(r+1)/2 <= t' <
+    // (r+1)(r+2)/2, at column b = dp-1-(t' - r(r+1)/2).  Each lane loads
+    // four blocks before it stores any.
+    for (int t0 = 0; t0 < nblk; t0 += 128) {
+        float4 u[4], v[4];
+#pragma unroll
+        for (int s4 = 0; s4 < 4; ++s4) {
+            const int t = t0 + lane + 32 * s4;
+            u[s4] = v[s4] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (t < nblk) {
+                u[s4] = __ldg(rec4 + 2 * t);
+                v[s4] = __ldg(rec4 + 2 * t + 1);
+            }
+        }
+#pragma unroll
+        for (int s4 = 0; s4 < 4; ++s4) {
+            const int t = t0 + lane + 32 * s4;
+            if (t >= nblk) continue;
+            const int tr = nblk - 1 - t;
+            const int r = (int)((sqrtf((float)(8 * tr + 1)) - 1.f) * 0.5f);
+            const int a = dp - 1 - r, b = dp - 1 - (tr - r * (r + 1) / 2);
+            const int i0 = 2 * a, i1 = 2 * a + 1, j0 = 2 * b, j1 = 2 * b + 1;
+            if (j0 < n) Cm[i0 * LD + j0] = cmk<float>(u[s4].x, u[s4].y);
+            if (j1 < n) Cm[i0 * LD + j1] = cmk<float>(u[s4].z, u[s4].w);
+            if (i1 < n && j0 >= i1) Cm[i1 * LD + j0] = cmk<float>(v[s4].x, v[s4].y);
+            if (j1 < n) Cm[i1 * LD + j1] = cmk<float>(v[s4].z, v[s4].w);
+        }
     }
     __syncwarp();
     if (!NORMALIZE) return info;
