@@ -355,6 +355,38 @@ def nmap_measurement(stack, d_stack, ctx, steps, cpu_rows):
     return res
 
 
+def integrate_ps_measurement(d_stack, ctx, steps, hbm_peak, seed=5):
+    """The PS/DS merge downstream of phase linking (fpl_integrate_ps,
+    python/integratePS.py) on the same scene: the stack serves as both the
+    phase-linked and the SLC stack, 10% of the pixels are PS.  HBM-bound:
+    per pixel the PS flag, tcorr and one stack (8N bytes) are read and the
+    N-1 interferograms and tcorr written, 16N + 1 bytes; timed with CUDA
+    events on the launching stream over `steps` launches."""
+    import torch
+    from fringe_gb300 import integrate_ps
+    nb, R, C = d_stack.shape
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    ps = (torch.rand((R, C), generator=g, device="cuda") < 0.1).to(torch.uint8)
+    tc = torch.rand((R, C), generator=g, device="cuda")
+    for _ in range(3):
+        integrate_ps(d_stack, d_stack, tc, ps, ctx=ctx)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(steps):
+        integrate_ps(d_stack, d_stack, tc, ps, ctx=ctx)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    alg = float(R * C * (16 * nb + 1))
+    return {"workload": "single-master PS/DS merge of the %dx%d N=%d scene, 10%% PS pixels" % (R, C, nb),
+            "value": R * C / (ms / 1e3), "unit": "px/s", "ms_per_step": ms,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / hbm_peak,
+                         "work": "16N+1 bytes per pixel"}}
+
+
 def batch_measurement(stack, nmap, seed=7):
     """Uneven ministacks in one batched launch sequence (replayed CUDA graph):
     16 tiles of 512^2..2048^2 pixels cut from the scene, ministacks of
@@ -640,6 +672,7 @@ def main():
         line["illconditioned"] = illcond_measurement(ctx)
     if not args.no_nmap and world == 1:
         line["nmap"] = nmap_measurement(stack, d_stack, ctx, max(1, args.steps), 0 if args.no_cpu else 384)
+        line["integrate_ps"] = integrate_ps_measurement(d_stack, ctx, max(3, args.steps), hbm_peak)
     if not args.no_cpu:
         rows = args.cpu_rows or 480          # about 15 s on 16 host cores
         line["cpu_baseline"] = cpu_baseline(stack, nmap, args.method, min(rows, R))

@@ -8,10 +8,12 @@ temporal coherence) runs as CUDA kernels behind the C ABI declared in
 * ``phase_link(stack, nmap, half_window, ...)`` -- in-memory run;
 * ``nmap(stack, half_window, prob=0.05, ...)`` -- the SHP bitmask (nmap
   module, two-sample KS test) that phase linking consumes;
+* ``integrate_ps(ds, slc, tcorr, ps)`` -- the PS/DS merge of the
+  integratePS workflow step (single-master interferograms, PS coherence);
 * ``evdlib.Evd`` / ``phase_linklib.Phaselink`` -- drop-in replacements of the
   reference's module wrappers (file level);
 * ``synth`` -- seeded synthetic stacks and SHP bitmasks.
 """
-from .linker import nmap, phase_link  # noqa: F401
+from .linker import integrate_ps, nmap, phase_link  # noqa: F401
 
-__all__ = ["phase_link", "nmap"]
+__all__ = ["phase_link", "nmap", "integrate_ps"]

@@ -44,6 +44,13 @@ class FplNmapJob(ctypes.Structure):
                 ("nmap", ctypes.c_void_p), ("count", ctypes.c_void_p)]
 
 
+class FplPsJob(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int), ("cols", ctypes.c_int), ("nbands", ctypes.c_int),
+                ("master", ctypes.c_int), ("ds", ctypes.c_void_p), ("slc", ctypes.c_void_p),
+                ("tcorr", ctypes.c_void_p), ("ps", ctypes.c_void_p), ("ifg", ctypes.c_void_p),
+                ("tcorr_out", ctypes.c_void_p)]
+
+
 class FplServerConfig(ctypes.Structure):
     _fields_ = [("memory_budget", ctypes.c_size_t), ("wave_pixels", ctypes.c_longlong),
                 ("device", ctypes.c_int)]
@@ -99,6 +106,7 @@ _SIGS = {
                                        ctypes.POINTER(ctypes.c_int)]),
     "fpl_ctx_profile_kernels": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "fpl_nmap": (ctypes.c_int, [_P, ctypes.POINTER(FplNmapJob)]),
+    "fpl_integrate_ps": (ctypes.c_int, [_P, ctypes.POINTER(FplPsJob), _P]),
 }
 _EXTRA = {}
 

@@ -20,7 +20,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC"]
 
 SOURCES = ["api.cu", "kernels_f32.cu", "kernels_f64.cu", "gram_box.cu", "batch.cu", "serve.cu", "noalloc.cu",
-           "nmap.cu", "io.cpp"]
+           "nmap.cu", "integrate.cu", "io.cpp"]
 
 
 def _nvcc():

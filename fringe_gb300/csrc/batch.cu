@@ -67,16 +67,14 @@ template <int NP>
 __global__ void k_batch_fp64(const BatchEntry *__restrict__ jobs, int njobs)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int warps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char *sm = smem + (size_t)warp * Lay<double, NP>::bytes;
-    const long long gw = (long long)blockIdx.x * warps + warp;
-    const long long nw = (long long)gridDim.x * warps;
     for (int j = 0; j < njobs; ++j) {
         const KParams &P = jobs[j].P;
         int cnt = *((volatile int *)P.fb_count);
         cnt = cnt < P.fb_cap ? cnt : P.fb_cap;
-        for (long long q = gw; q < cnt; q += nw) process_pixel<double, NP>(P, P.fb_list[q], sm, lane);
+        for (long long q = fb_next(P, lane); q < cnt; q = fb_next(P, lane))
+            process_pixel<double, NP>(P, P.fb_list[q], sm, lane);
     }
 }
 

@@ -7,7 +7,8 @@
 //                        FP32 rounding band), or over every pixel when no list
 //                        is given (used to check the FP64 form itself).
 // Both are persistent: the grid is sized to the resident capacity of the
-// GPU and warps stride over their pixels.
+// GPU; warps stride over a pixel range, or draw work-list entries from a
+// cursor.
 #pragma once
 #include <type_traits>
 #include "kernels.h"
@@ -29,7 +30,8 @@ __global__ void k_pixels(KParams P)
     } else {
         int cnt = *((volatile int *)P.fb_count);
         cnt = cnt < P.fb_cap ? cnt : P.fb_cap;
-        for (long long q = gw; q < cnt; q += nw) process_pixel<T, NP>(P, P.fb_list[q], sm, lane);
+        for (long long q = fb_next(P, lane); q < cnt; q = fb_next(P, lane))
+            process_pixel<T, NP>(P, P.fb_list[q], sm, lane);
     }
 }
 

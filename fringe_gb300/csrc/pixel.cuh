@@ -44,7 +44,8 @@ struct KParams {
     int method, semantics, mini, bw, min_neigh;
     float amb;                          // width of the FP32 rounding band, in units of n*eps*|A|_F
     float cond_max;                     // largest inf-norm condition of |C| inverted in FP32
-    int *fb_count;                      // FP64 work list (scratch)
+    int *fb_count;                      // FP64 work list (scratch): the 64-byte counter block of the
+                                        // run: +0 list length, +16 err, +32 slow, +48 work cursor
     long long *fb_list;
     int fb_cap;
     unsigned *err;                      // error flags (scratch)
@@ -1130,6 +1131,16 @@ __device__ __forceinline__ void acc_prod<double>(C2<double> &acc, float2 a, floa
     float im = __fsub_rn(__fmul_rn(a.y, b.x), __fmul_rn(a.x, b.y));
     acc.x += double(re);
     acc.y += double(im);
+}
+
+// next entry of the FP64 work list for this warp: warps draw entries from a
+// cursor in the run's counter block (zeroed with it), so the SMs whose
+// pixels were cheap take more of them
+__device__ __forceinline__ long long fb_next(const KParams &P, int lane)
+{
+    int q = 0;
+    if (lane == 0) q = atomicAdd(P.fb_count + 12, 1);
+    return __shfl_sync(0xffffffffu, q, 0);
 }
 
 __device__ __forceinline__ void defer_fp64(const KParams &P, long long pp, int lane)

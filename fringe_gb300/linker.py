@@ -194,3 +194,54 @@ def nmap(stack, half_window, prob=0.05, mask=None, amp_const=None, device=0, out
                           out["nmap"].ctypes.data, out["count"].ctypes.data)
     _lib.check(lib.fpl_nmap(ctx.handle, ctypes.byref(job)), ctx.handle)
     return out
+
+
+def integrate_ps(ds, slc, tcorr, ps, master=0, device=0, ctx=None):
+    """PS/DS merge of python/integratePS.py over the single-master network
+    (python/Network.py:95-104): for every band j != master, in band order,
+    ds_j * conj(ds_master), replaced at PS pixels (ps == 1) by
+    exp(1j * angle(slc_j * conj(slc_master))); and tcorr with PS pixels set
+    to 0.95.
+
+    ds, slc : complex64 [nbands, rows, cols] (phase-linked and original
+    stacks); tcorr : float32 [rows, cols]; ps : [rows, cols] PS map.  NumPy
+    arrays (copied through the device) or CUDA torch tensors.  Returns
+    dict(ifg complex64 [nbands-1, rows, cols], tcorr float32 [rows, cols]),
+    of the inputs' kind.
+    """
+    import torch
+    ctx = ctx or _lib.context(device)
+    lib = _lib.load()
+    host = not _is_torch(ds)
+    dev = torch.device("cuda", ctx.device) if host else ds.device
+
+    def on_dev(a, dt):
+        if _is_torch(a):
+            if not a.is_cuda:
+                raise ValueError("torch inputs must be CUDA tensors (use NumPy for host memory)")
+            return a.to(dt).contiguous()
+        return torch.from_numpy(np.ascontiguousarray(a)).to(device=dev, dtype=dt)
+
+    d_ds = on_dev(ds, torch.complex64)
+    d_slc = on_dev(slc, torch.complex64)
+    d_tc = on_dev(tcorr, torch.float32)
+    # the reference tests psPixels == 1 in the map's own type
+    if _is_torch(ps):
+        d_ps = ps.contiguous() if ps.dtype == torch.uint8 else (ps == 1).to(torch.uint8)
+        d_ps = on_dev(d_ps, torch.uint8)
+    else:
+        p_np = np.asarray(ps)
+        d_ps = on_dev(p_np if p_np.dtype == np.uint8 else (p_np == 1).astype(np.uint8), torch.uint8)
+    nb, R, C = d_ds.shape
+    if tuple(d_slc.shape) != (nb, R, C) or tuple(d_tc.shape) != (R, C) or tuple(d_ps.shape) != (R, C):
+        raise ValueError("ds, slc must be [nbands, rows, cols] and tcorr, ps [rows, cols]")
+    ifg = torch.empty((max(nb - 1, 0), R, C), dtype=torch.complex64, device=dev)
+    tc_out = torch.empty((R, C), dtype=torch.float32, device=dev)
+    job = _lib.FplPsJob(R, C, nb, int(master), d_ds.data_ptr(), d_slc.data_ptr(), d_tc.data_ptr(),
+                        d_ps.data_ptr(), ifg.data_ptr() if ifg.numel() else None, tc_out.data_ptr())
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(lib.fpl_integrate_ps(ctx.handle, ctypes.byref(job), ctypes.c_void_p(stream)), ctx.handle)
+    if host:
+        torch.cuda.synchronize(dev)
+        return {"ifg": ifg.cpu().numpy(), "tcorr": tc_out.cpu().numpy()}
+    return {"ifg": ifg, "tcorr": tc_out}

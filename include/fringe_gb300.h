@@ -309,6 +309,28 @@ int fpl_process(const fpl_options *opts);
 int fpl_adjust_wrapped(fpl_ctx *ctx, const void *phase, const void *datum, void *out,
                        int ndates, long long npix, void *stream);
 
+/* PS/DS merge of python/integratePS.py (integratePS2DS :94-126,
+ * get_fullres_ifgram :66-75, getCoherence :129-152) over the single-master
+ * network of python/Network.py:95-104.  For every band j != master, in band
+ * order (output slot q = j - (j > master)):
+ *   ifg[q][p] = ds[j][p] * conj(ds[master][p])                      (DS pixel)
+ *             = exp(1j * angle(slc[j][p] * conj(slc[master][p])))  (ps[p] == 1)
+ * and tcorr_out[p] = 0.95 at PS pixels, tcorr[p] elsewhere.  Device
+ * pointers; enqueued on `stream` (NULL = the legacy default stream).
+ * tcorr_out may alias tcorr; ifg must not overlap the inputs.  An empty
+ * scene (rows or cols 0) returns FPL_OK without reading any pointer. */
+typedef struct fpl_ps_job {
+    int rows, cols, nbands;
+    int master;                  /* band of the reference date (the first date: 0) */
+    const void *ds;              /* complex64 [nbands][rows][cols], phase-linked stack */
+    const void *slc;             /* complex64 [nbands][rows][cols], SLC stack          */
+    const float *tcorr;          /* [rows][cols] temporal coherence                   */
+    const uint8_t *ps;           /* [rows][cols] PS map, 1 = PS pixel                 */
+    void *ifg;                   /* complex64 [nbands-1][rows][cols]                  */
+    float *tcorr_out;            /* [rows][cols]                                      */
+} fpl_ps_job;
+int fpl_integrate_ps(fpl_ctx *ctx, const fpl_ps_job *job, void *stream);
+
 /* Human-readable text for a return code. */
 const char *fpl_error_string(int code);
 
