@@ -608,7 +608,9 @@ __device__ bool warp_sweep_inverse(T *A, int n, T *rowk, T *inf_norm, int lane)
 // buffer and every lane updates its own row from it, so the matrix is read
 // from shared memory once and written back once instead of at every step.
 // Same sweep as warp_sweep_inverse; the pivot row's update is written
-// x + (1/p - 1) x.  rowb: 2 x NP floats of shared memory (16-byte aligned).
+// x + (1/p - 1) x.  The loop over k is not unrolled (its body is the same
+// for every k), which keeps the code small.  rowb: 2 x NP + 2 floats of
+// shared memory (16-byte aligned): two row buffers and two pivot slots.
 template <int LD, int NP>
 __device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf_norm, int lane)
 {
@@ -616,42 +618,38 @@ __device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf
     float x[NP];
 #pragma unroll
     for (int j = 0; j < NP; ++j) x[j] = (lane < n && j < n) ? A[lane * LD + j] : 0.f;
-    // k = 8 kb + ku with ku unrolled, so column k's register is one of
-    // NP / 8 candidates
-    for (int kb = 0; kb < NP / 8; ++kb) {
-        if (8 * kb >= n) break;
+    // Lane k publishes row k with its k-th entry replaced by p - 1 (p, the
+    // pivot a_kk, is kept beside the row): x + (-f)(p - 1) turns a_ik into
+    // a_ik / p = f in the same fused multiply-add as the rest of the row,
+    // so column k needs no register chosen by k.  Lane k's own entry
+    // becomes 2 - 1/p instead of -1/p; no later step reads a row's
+    // diagonal after that row was swept, and the 2 is taken off at the end.
+#pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        float *rk = rowb + (k & 1) * NP;
+        float *pk = rowb + 2 * NP + (k & 1);
+        if (lane == k) {
 #pragma unroll
-        for (int ku = 0; ku < 8; ++ku) {
-            const int k = 8 * kb + ku;
-            if (k >= n) break;
-            float *rk = rowb + (ku & 1) * NP;
-            if (lane == k) {
+            for (int j = 0; j < NP; j += 4) *reinterpret_cast<float4 *>(rk + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+            const float v = rk[k];
+            *pk = v;
+            rk[k] = v - 1.f;
+        }
+        __syncwarp();
+        const float p = *pk;
+        if (!(p > 0.f)) return false;
+        const float rp = 1.f / p;
+        const bool own = (lane == k);
+        // row k: a_kj / p;  other rows: a_ij - (a_ik / p) a_kj  (a_ik = a_ki)
+        const float f = ((lane < NP) ? rk[lane] : 0.f) * rp;
+        const float bm = own ? rp - 1.f : -f;
 #pragma unroll
-                for (int j = 0; j < NP; j += 4) *reinterpret_cast<float4 *>(rk + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
-            }
-            __syncwarp();
-            const float p = rk[k];
-            if (!(p > 0.f)) return false;
-            const float rp = 1.f / p;
-            const bool own = (lane == k);
-            // row k: a_kj / p;  other rows: a_ij - (a_ik / p) a_kj  (a_ik = a_ki).
-            // Lane k published its own row (r = x), so one fused multiply-add
-            // serves both: x + (1/p - 1) x on lane k, x - f r elsewhere.
-            const float f = ((lane < NP) ? rk[lane] : 0.f) * rp;
-            const float bm = own ? rp - 1.f : -f;
-#pragma unroll
-            for (int j = 0; j < NP; j += 4) {
-                const float4 r = *reinterpret_cast<const float4 *>(rk + j);
-                x[j] = fmaf(bm, r.x, x[j]);
-                x[j + 1] = fmaf(bm, r.y, x[j + 1]);
-                x[j + 2] = fmaf(bm, r.z, x[j + 2]);
-                x[j + 3] = fmaf(bm, r.w, x[j + 3]);
-            }
-            // column k: x[k] = own ? -1/p : a_ik / p
-            const float vk = own ? -rp : f;
-#pragma unroll
-            for (int b = 0; b < NP / 8; ++b)
-                if (kb == b) x[8 * b + ku] = vk;
+        for (int j = 0; j < NP; j += 4) {
+            const float4 r = *reinterpret_cast<const float4 *>(rk + j);
+            x[j] = fmaf(bm, r.x, x[j]);
+            x[j + 1] = fmaf(bm, r.y, x[j + 1]);
+            x[j + 2] = fmaf(bm, r.z, x[j + 2]);
+            x[j + 3] = fmaf(bm, r.w, x[j + 3]);
         }
     }
     __syncwarp();
@@ -660,7 +658,7 @@ __device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf
 #pragma unroll
         for (int j = 0; j < NP; ++j) {
             if (j < n) {
-                const float v = -x[j];
+                const float v = (j == lane) ? 2.f - x[j] : -x[j];
                 A[lane * LD + j] = v;
                 s += fabsf(v);
             }
