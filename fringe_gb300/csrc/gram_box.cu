@@ -71,6 +71,10 @@ template <int KC> struct BoxLay {
     static constexpr size_t MAX_SMEM = OFF_U + (size_t)BX_M * BX_MAXW * 4;
 };
 
+// union samples of a tile: (8 + 2 ny) rows of (16 + 2 nx) samples, packed
+// row after row (no padding: every sample slot is a GEMM K index)
+__host__ __device__ __forceinline__ int box_union_cols(int nx) { return BX_TC + 2 * nx; }
+
 __device__ __forceinline__ uint32_t smem_addr(const void *p)
 {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -235,7 +239,7 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
     const int n = P.nb, dp = (n + 1) >> 1, nblk = dp * (dp + 1) / 2, ncolt = 8 * nblk;
     const int cols = P.cols, rows = P.rows, nul = P.nulong;
     const int wy = 2 * P.ny + 1, wx = P.wx;
-    const int uh = BX_TR + wy - 1, uw = BX_TC + wx - 1, uwp = (uw + 7) & ~7;
+    const int uh = BX_TR + wy - 1, uw = BX_TC + wx - 1, uwp = box_union_cols(P.nx);
     const int kp = (uh * uwp + KC - 1) / KC * KC, nchunk = kp / KC;
     const int W = kp >> 5;
     const int ra = int(P.pix_begin / cols), rb = ra + int(P.npix / cols);
@@ -576,7 +580,7 @@ template <int KC>
 size_t box_smem(int ny, int nx)
 {
     using L = BoxLay<KC>;
-    const int uh = BX_TR + 2 * ny, uwp = (BX_TC + 2 * nx + 7) & ~7;
+    const int uh = BX_TR + 2 * ny, uwp = box_union_cols(nx);
     const int kp = (uh * uwp + KC - 1) / KC * KC;
     return L::OFF_U + (size_t)BX_M * (kp / 32) * 4;
 }
@@ -632,7 +636,7 @@ bool gram_box_supported(int nb, int ny, int nx)
 {
     const int wx = 2 * nx + 1;
     if (nb < 1 || nb > 64 || wx > BX_MAXWX) return false;
-    const int uh = BX_TR + 2 * ny, uwp = (BX_TC + wx - 1 + 7) & ~7;
+    const int uh = BX_TR + 2 * ny, uwp = box_union_cols(nx);
     return (long long)uh * uwp <= BX_MAXK;
 }
 
