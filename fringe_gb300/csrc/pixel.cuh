@@ -1604,7 +1604,11 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             C2<T> m0, m1;
             warp_matvec<T, LD, NP>(Wm, n, vv, m0, m1, lane);
             const T rho0 = warp_sum(ccmul(z0, m0).x + ccmul(z1, m1).x);
-            const T sigma = T(0.98) * min(rho0, T(1));
+            // 1% below the Rayleigh quotient (or 1); if M - sigma I is not
+            // positive definite the shift was above lambda_1 and a second
+            // attempt backs off to 3% below
+            const T rho1 = min(rho0, T(1));
+            const T sigma = T(0.99) * rho1;
             __syncwarp();
             if (sigma > thr + dM) {
                 // one call site for the iteration and for rebuilding M (the
@@ -1620,13 +1624,19 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
                         abs_inverse();
                         form_M();
                     }
-                    if (st != 0 || attempt == 1) break;
-                    // slow: shift again just below the current Rayleigh
-                    // quotient (lambda_1 >= rho - res when the iterate is
-                    // closest to v_1; the Cholesky test verifies the shift)
+                    if (st == 1 || attempt == 1) break;
                     if (lane == 0) atomicAdd(P.slow, 1);
-                    const T sigma1 = lam - T(2) * res;
-                    if (!(sigma1 > sig && sigma1 > thr + dM)) {
+                    T sigma1;
+                    if (st == 0) {
+                        // slow: shift again just below the current Rayleigh
+                        // quotient (lambda_1 >= rho - res when the iterate is
+                        // closest to v_1; the Cholesky test verifies the shift)
+                        sigma1 = lam - T(2) * res;
+                        if (!(sigma1 > sig)) sigma1 = T(0);
+                    } else {
+                        sigma1 = T(0.97) * rho1;
+                    }
+                    if (!(sigma1 > thr + dM)) {
                         st = -1;
                         break;
                     }

@@ -126,7 +126,7 @@ typedef struct {
     long long pixels;            /* pixels in the row range          */
     long long fp64_pixels;       /* pixels settled by the FP64 path  */
     long long mixed_fp64_inverse;/* MLE pixels whose |G| inverse ran in FP64 */
-    long long slow_path_pixels;  /* pixels whose eigenvector needed the Householder path */
+    long long slow_path_pixels;  /* pixels that left the fast eigen path (second shift or Householder) */
     float kernel_ms;             /* device time of the compute kernels */
     float total_ms;              /* wall time of the call             */
 } fpl_stats;
