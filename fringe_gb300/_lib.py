@@ -98,6 +98,7 @@ _SIGS = {
                                        ctypes.POINTER(FplTicketInfo)]),
     "fpl_server_destroy": (ctypes.c_int, [_P]),
     "fpl_ctx_set_tuning": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
+    "fpl_ctx_set_shift": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float]),
     "fpl_adjust_wrapped": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_longlong, _P]),
     "fpl_ctx_last_error": (ctypes.c_char_p, [_P]),
     "fpl_ctx_set_profiling": (ctypes.c_int, [_P, ctypes.c_int]),
@@ -203,6 +204,10 @@ class Context:
 
     def set_tuning(self, amb_scale=-1.0, force_fp64=False):
         check(load().fpl_ctx_set_tuning(self.handle, float(amb_scale), int(force_fp64)), self.handle)
+
+    def set_shift(self, shift=0.99, backoff=0.97):
+        """Shifts of the FP32 MLE inverse iteration (fpl_ctx_set_shift)."""
+        check(load().fpl_ctx_set_shift(self.handle, float(shift), float(backoff)), self.handle)
 
 
 _contexts = {}

@@ -245,6 +245,8 @@ static int fpl_enqueue_body(fpl_ctx *ctx, const fpl_job *job, const void *stack,
     P.min_neigh = job->min_neighbors;
     P.amb = ctx->amb_scale;
     P.cond_max = ctx->cond_max;
+    P.shift = ctx->shift;
+    P.shift_backoff = ctx->shift_backoff;
     int *d_count = reinterpret_cast<int *>(counters);
     unsigned *d_err = reinterpret_cast<unsigned *>(static_cast<char *>(counters) + 16);
     P.fb_count = d_count;
@@ -467,6 +469,15 @@ int fpl_ctx_set_tuning(fpl_ctx *ctx, float amb_scale, int force_fp64)
     if (!ctx) return FPL_ERR_NULL;
     if (amb_scale >= 0.f) ctx->amb_scale = amb_scale;
     ctx->force_fp64 = force_fp64 != 0;
+    return FPL_OK;
+}
+
+int fpl_ctx_set_shift(fpl_ctx *ctx, float shift, float backoff)
+{
+    if (!ctx) return FPL_ERR_NULL;
+    if (!(shift > 0.f) || !(backoff > 0.f)) return FPL_ERR_OPTIONS;
+    ctx->shift = shift;
+    ctx->shift_backoff = backoff;
     return FPL_OK;
 }
 

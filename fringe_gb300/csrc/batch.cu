@@ -216,6 +216,8 @@ void fill_params(KParams &P, const fpl_job &jb, int r0, int r1, float amb, float
     P.min_neigh = jb.min_neighbors;
     P.amb = amb;
     P.cond_max = cond_max;
+    P.shift = kDefaultShift;
+    P.shift_backoff = kDefaultShiftBackoff;
 }
 
 }  // namespace fpl
@@ -391,6 +393,8 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
         const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
         fpl::KParams &P = table[e].P;
         fpl::fill_params(P, jb, r0, r1, ctx->amb_scale, ctx->cond_max);
+        P.shift = ctx->shift;
+        P.shift_backoff = ctx->shift_backoff;
         set_counters(P, e);
         b->job_of_entry.push_back(j);
     }
@@ -432,6 +436,8 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
             const fpl_job &jb = jobs[pc.job];
             fpl::KParams &P = pp[i];
             fpl::fill_params(P, jb, pc.ra, pc.rb, ctx->amb_scale, ctx->cond_max);
+            P.shift = ctx->shift;
+            P.shift_backoff = ctx->shift_backoff;
             set_counters(P, nf + i);
             P.cbuf = reinterpret_cast<float2 *>(recs + rec_off[i]);
             P.cinfo = infos + info_off[i];

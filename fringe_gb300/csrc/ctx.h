@@ -17,6 +17,8 @@ constexpr size_t kCounterBlock = 64;
 // default tuning of the FP32 form
 constexpr float kDefaultAmbScale = 8.0f;    // FP32 rounding band, in units of n*eps*|A|_F
 constexpr float kDefaultCondMax = 1000.0f;  // |C| inverted in FP32 up to this inf-norm condition
+constexpr float kDefaultShift = 0.99f;      // inverse-iteration shift, in units of min(1, rho)
+constexpr float kDefaultShiftBackoff = 0.97f;   // second shift when M - sigma I is not definite
 
 struct fpl_ctx {
     int device = 0;
@@ -45,6 +47,7 @@ struct fpl_ctx {
     // tuning
     float amb_scale = kDefaultAmbScale;
     float cond_max = kDefaultCondMax;
+    float shift = kDefaultShift, shift_backoff = kDefaultShiftBackoff;
     bool force_fp64 = false;
     // optional per-kernel timing: an event pair around every compute launch,
     // tagged with the kernel (enum fpl_kernel_tag)

@@ -105,6 +105,8 @@ extern "C" int fpl_run_noalloc(const fpl_job *job, void *stream)
     P.min_neigh = job->min_neighbors;
     P.amb = kDefaultAmbScale;
     P.cond_max = kDefaultCondMax;
+    P.shift = kDefaultShift;
+    P.shift_backoff = kDefaultShiftBackoff;
     P.fb_count = reinterpret_cast<int *>(scratch);
     P.err = reinterpret_cast<unsigned *>(scratch + 16);
     P.slow = reinterpret_cast<int *>(scratch + 32);

@@ -44,6 +44,7 @@ struct KParams {
     int method, semantics, mini, bw, min_neigh;
     float amb;                          // width of the FP32 rounding band, in units of n*eps*|A|_F
     float cond_max;                     // largest inf-norm condition of |C| inverted in FP32
+    float shift, shift_backoff;         // inverse-iteration shifts, in units of min(1, rho)
     int *fb_count;                      // FP64 work list (scratch): the 64-byte counter block of the
                                         // run: +0 list length, +16 err, +32 slow, +48 work cursor
     long long *fb_list;
@@ -1604,11 +1605,11 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             C2<T> m0, m1;
             warp_matvec<T, LD, NP>(Wm, n, vv, m0, m1, lane);
             const T rho0 = warp_sum(ccmul(z0, m0).x + ccmul(z1, m1).x);
-            // 1% below the Rayleigh quotient (or 1); if M - sigma I is not
-            // positive definite the shift was above lambda_1 and a second
-            // attempt backs off to 3% below
+            // P.shift (1%) below the Rayleigh quotient (or 1); if M - sigma I
+            // is not positive definite the shift was above lambda_1 and a
+            // second attempt backs off to P.shift_backoff (3%) below
             const T rho1 = min(rho0, T(1));
-            const T sigma = T(0.99) * rho1;
+            const T sigma = T(P.shift) * rho1;
             __syncwarp();
             if (sigma > thr + dM) {
                 // one call site for the iteration and for rebuilding M (the
@@ -1634,7 +1635,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
                         sigma1 = lam - T(2) * res;
                         if (!(sigma1 > sig)) sigma1 = T(0);
                     } else {
-                        sigma1 = T(0.97) * rho1;
+                        sigma1 = T(P.shift_backoff) * rho1;
                     }
                     if (!(sigma1 > thr + dM)) {
                         st = -1;

@@ -225,6 +225,13 @@ const char *fpl_ctx_last_error(const fpl_ctx *ctx);
 /* Tuning hooks: width of the FP32 rounding band (in units of n*eps*|A|_F,
  * < 0 keeps the current value) and FP64 for every pixel (test use). */
 int fpl_ctx_set_tuning(fpl_ctx *ctx, float amb_scale, int force_fp64);
+/* Shifts of the FP32 MLE inverse iteration, as fractions of min(1, rho) (rho
+ * the Rayleigh quotient of the start vector): the first attempt and the
+ * second one made when M - sigma I is not positive definite (defaults 0.99,
+ * 0.97).  A shift above 1 makes that attempt fail, which is how tests reach
+ * the second attempt and the Householder path.  Runs and batches on this
+ * context use them (servers and fpl_run_noalloc keep the defaults). */
+int fpl_ctx_set_shift(fpl_ctx *ctx, float shift, float backoff);
 /* Per-kernel device timing of subsequent runs (CUDA events on the run's
  * stream); fpl_ctx_profile waits for them, returns the summed FP32 and FP64
  * kernel milliseconds and the run count, and resets the record. */

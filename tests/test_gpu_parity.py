@@ -124,6 +124,29 @@ def test_fp64_form_matches_oracle_tightly(gpu_lib, vor30):
     ctx.close()
 
 
+@pytest.mark.parametrize("shift,backoff", [(1.5, 0.97), (1.5, 1.5)])
+def test_mle_fallback_paths(gpu_lib, vor30, shift, backoff):
+    """A first shift above lambda_1 makes the Cholesky of M - sigma I fail:
+    (1.5, 0.97) takes the second attempt at the backed-off shift, (1.5, 1.5)
+    fails both and takes the Householder path; both agree with the oracle."""
+    from fringe_gb300 import _lib, phase_link
+    stack, nmap = vor30
+    ctx = _lib.Context(0)
+    ctx.set_shift(shift, backoff)
+    for prec in ("fp32", "mixed"):
+        for sem in ("evd", "phase_link"):
+            g = phase_link(stack, nmap, (5, 10), method="MLE", semantics=sem, precision=prec,
+                           want_status=True, ctx=ctx)
+            o = oracle.run(stack, nmap, 5, 10, method="MLE", semantics=sem)
+            m = compare(g, o)
+            assert m["valid_both"] > 1000, m
+            assert_parity(m)
+    # host-memory run: the statistics count the pixels that left the fast path
+    phase_link(stack, nmap, (5, 10), method="MLE", ctx=ctx)
+    assert ctx.stats()["slow_path_pixels"] > 1000
+    ctx.close()
+
+
 def test_row_range_and_torch_device_path(gpu_lib, vor30):
     torch = pytest.importorskip("torch")
     from fringe_gb300 import phase_link
