@@ -69,13 +69,20 @@ __global__ void k_batch_fp64(const BatchEntry *__restrict__ jobs, int njobs)
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char *sm = smem + (size_t)warp * Lay<double, NP>::bytes;
+    __shared__ uint32_t tslot;
+    uint32_t tbase = 0, taddr = 0;
+    if constexpr (CInTmem<double, NP>::value) {
+        tbase = tmem_alloc_cta(&tslot, warp, 512);
+        taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
+    }
     for (int j = 0; j < njobs; ++j) {
         const KParams &P = jobs[j].P;
         int cnt = *((volatile int *)P.fb_count);
         cnt = cnt < P.fb_cap ? cnt : P.fb_cap;
         for (long long q = fb_next(P, lane); q < cnt; q = fb_next(P, lane))
-            process_pixel<double, NP>(P, P.fb_list[q], sm, lane);
+            process_pixel<double, NP>(P, P.fb_list[q], sm, lane, taddr);
     }
+    if constexpr (CInTmem<double, NP>::value) tmem_free_cta(tbase, warp, 512);
 }
 
 __global__ void k_popcount(const uint32_t *__restrict__ w, long long nwords, unsigned long long *sum)
@@ -119,6 +126,7 @@ int max_warps(int np, bool fp64)
 {
     const size_t per = warp_bytes(np, fp64);
     int w = per ? int((224 * 1024) / per) : 1;
+    if (fp64 && np == 64) w = std::min(w, 4);   // C in tensor memory: one lane quadrant per warp
     return std::max(1, std::min(w, 16));
 }
 

@@ -25,14 +25,22 @@ __global__ void k_pixels(KParams P)
     unsigned char *sm = smem + (size_t)warp * Lay<T, NP>::bytes;
     const long long gw = (long long)blockIdx.x * warps + warp;
     const long long nw = (long long)gridDim.x * warps;
+    // FP64 at 64 dates: C in tensor memory, one lane quadrant per warp
+    __shared__ uint32_t tslot;
+    uint32_t tbase = 0, taddr = 0;
+    if constexpr (CInTmem<T, NP>::value) {
+        tbase = tmem_alloc_cta(&tslot, warp, 512);
+        taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
+    }
     if (sizeof(T) == 4 || P.fb_list == nullptr) {
-        for (long long q = gw; q < P.npix; q += nw) process_pixel<T, NP>(P, P.pix_begin + q, sm, lane);
+        for (long long q = gw; q < P.npix; q += nw) process_pixel<T, NP>(P, P.pix_begin + q, sm, lane, taddr);
     } else {
         int cnt = *((volatile int *)P.fb_count);
         cnt = cnt < P.fb_cap ? cnt : P.fb_cap;
         for (long long q = fb_next(P, lane); q < cnt; q = fb_next(P, lane))
-            process_pixel<T, NP>(P, P.fb_list[q], sm, lane);
+            process_pixel<T, NP>(P, P.fb_list[q], sm, lane, taddr);
     }
+    if constexpr (CInTmem<T, NP>::value) tmem_free_cta(tbase, warp, 512);
 }
 
 // mixed form, second half: eigen-solves from the tensor-core Gamma records.
@@ -251,6 +259,7 @@ static cudaError_t launch_t(const KParams &P, int num_sms, cudaStream_t st)
     const size_t budget = 224 * 1024;   // of the 227 KB a block may opt into
     int warps = int(budget / per_warp);
     if (warps > 16) warps = 16;
+    if (CInTmem<T, NP>::value && warps > 4) warps = 4;   // one tensor-memory lane quadrant per warp
     if (warps < 1) warps = 1;
     const size_t smem = per_warp * warps;
     int dev = 0;

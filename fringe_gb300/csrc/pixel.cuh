@@ -174,6 +174,39 @@ template <typename T, int NP> struct Lay {
     static constexpr size_t bytes = cm + align16(mat);
 };
 
+// FP64 at 64 dates keeps C in tensor memory during the eigen-solve (see
+// CInTmem), so the coherence needs shared memory only while Gamma is summed
+// and normalised: it sits right after the gather staging, over the work
+// matrix (which the solve uses only after C has been copied out), and the
+// vectors follow it.  91.6 KB per warp instead of 141 KB: two warps per SM.
+template <> struct Lay<double, 64> {
+    static constexpr int NP = 64;
+    static constexpr int LD = NP + 1;
+    static constexpr int XS = NP + 2;
+    static constexpr size_t mat = sizeof(C2<double>) * NP * LD;
+    static constexpr size_t wm = 0;
+    static constexpr size_t stage = align16(sizeof(float2) * 32 * XS);  // gather staging at wm
+    static constexpr size_t wm_bytes = align16(cmax(mat, stage));
+    static constexpr size_t xr = wm + align16(mat / 2);
+    static constexpr size_t cm = stage;                               // Gamma / C while it is formed
+    static constexpr size_t vv = cmax(wm + wm_bytes, cm + align16(mat));
+    static constexpr size_t ww = align16(vv + sizeof(C2<double>) * NP);
+    static constexpr size_t tu = align16(ww + sizeof(C2<double>) * NP);
+    static constexpr size_t dd = align16(tu + sizeof(C2<double>) * NP);
+    static constexpr size_t ee = align16(dd + sizeof(double) * NP);
+    static constexpr size_t e2 = align16(ee + sizeof(double) * NP);
+    static constexpr size_t yy = align16(e2 + sizeof(double) * NP);
+    static constexpr size_t wk = align16(yy + sizeof(double) * NP);
+    static constexpr size_t ph = align16(wk + sizeof(double) * 5 * NP);
+    static constexpr size_t bytes_noc = align16(ph + sizeof(float2) * NP);
+    static constexpr size_t bytes = bytes_noc;
+};
+
+// kernels whose warps hold C in tensor memory in the FP64 form
+template <typename T, int NP> struct CInTmem {
+    static constexpr bool value = sizeof(T) == 8 && NP == 64;
+};
+
 // ------------------------------------------------------------------------
 // Access to the rows of the coherence C.  Lane l owns rows l and l + 32;
 // rows are read and written in chunks of 8 complex entries (columns 8c ..
@@ -254,6 +287,72 @@ template <int NP> struct CRowsTmem {
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     }
 };
+
+// The same rows of an FP64 C: a complex double is four 32-bit columns, so
+// row slot h starts 4*NP columns after slot h-1 (at 64 dates the warp's
+// two row slots fill the 512 columns of its lane quadrant).
+template <int NP> struct CRowsTmemD {
+    static_assert(NP <= 64, "at most two rows per lane");
+    static constexpr uint32_t kColsPerWarp = 4u * NP * ((NP + 31) / 32);
+    uint32_t taddr;      // lane quadrant << 16 | first column of the warp
+    __device__ __forceinline__ void load(int h, int c, C2<double> (&v)[8]) const
+    {
+        const uint32_t a = taddr + (uint32_t)(4 * NP * h) + 32u * (uint32_t)c;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            uint32_t r[16];
+            tmem_ld16(a + 16u * (uint32_t)half, r);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                v[4 * half + k] = cmk<double>(__hiloint2double((int)r[4 * k + 1], (int)r[4 * k]),
+                                              __hiloint2double((int)r[4 * k + 3], (int)r[4 * k + 2]));
+        }
+    }
+    __device__ __forceinline__ void store(int h, int c, const C2<double> (&v)[8]) const
+    {
+        const uint32_t a = taddr + (uint32_t)(4 * NP * h) + 32u * (uint32_t)c;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            uint32_t r[16];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const C2<double> x = v[4 * half + k];
+                r[4 * k] = (uint32_t)__double2loint(x.x);
+                r[4 * k + 1] = (uint32_t)__double2hiint(x.x);
+                r[4 * k + 2] = (uint32_t)__double2loint(x.y);
+                r[4 * k + 3] = (uint32_t)__double2hiint(x.y);
+            }
+            tmem_st16(a + 16u * (uint32_t)half, r);
+        }
+    }
+    __device__ __forceinline__ void fence() const
+    {
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+};
+
+// tensor memory of a CTA: warp 0 allocates `cols` columns (a power of two
+// >= 32) and gives up the right to allocate more; every thread gets the base
+// address.  Call from every thread; tmem_free_cta releases them.
+__device__ __forceinline__ uint32_t tmem_alloc_cta(uint32_t *slot, int warp, uint32_t cols)
+{
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"((uint32_t)__cvta_generic_to_shared(slot)), "r"(cols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    return *slot;
+}
+__device__ __forceinline__ void tmem_free_cta(uint32_t tbase, int warp, uint32_t cols)
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(cols) : "memory");
+}
 
 // number of row slots (h) and 8-entry chunks (c) per lane
 template <int NP> struct RowShape {
@@ -1864,17 +1963,17 @@ __device__ int pixel_load_gamma(const KParams &P, long long pp, unsigned char *s
 
 // rows of the coherence matrix C in shared memory (ld NP+1, full storage)
 // into the row policy cp (every lane calls it together)
-template <int NP, typename CP>
-__device__ void rows_from_smem(const CP &cp, const C2<float> *A, int lane)
+template <int NP, typename CP, typename T>
+__device__ void rows_from_smem(const CP &cp, const C2<T> *A, int lane)
 {
 #pragma unroll
     for (int h = 0; h < RowShape<NP>::H; ++h) {
         const int i = lane + 32 * h;
 #pragma unroll 1
         for (int c = 0; c < RowShape<NP>::CH; ++c) {
-            C2<float> v[8];
+            C2<T> v[8];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) v[k] = (i < NP) ? A[i * (NP + 1) + 8 * c + k] : cmk<float>(0.f, 0.f);
+            for (int k = 0; k < 8; ++k) v[k] = (i < NP) ? A[i * (NP + 1) + 8 * c + k] : cmk<T>(T(0), T(0));
             cp.store(h, c, v);
         }
     }
@@ -1943,12 +2042,20 @@ __device__ bool rows_coherence(const KParams &P, long long pp, const C2<float> *
     return true;
 }
 
+// taddr: the warp's tensor-memory rows when CInTmem<T, NP> (C is formed in
+// shared memory, then moved there before the solve reuses that memory)
 template <typename T, int NP>
-__device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm, int lane)
+__device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm, int lane, uint32_t taddr = 0)
 {
     const int npix = pixel_coherence<T, NP>(P, pp, sm, lane);
-    if (npix >= 0) {
-        const CRowsSmem<T, NP> cp{reinterpret_cast<C2<T> *>(sm + Lay<T, NP>::cm), lane};
+    if (npix < 0) return;
+    const C2<T> *Cm = reinterpret_cast<const C2<T> *>(sm + Lay<T, NP>::cm);
+    if constexpr (CInTmem<T, NP>::value) {
+        const CRowsTmemD<NP> cp{taddr};
+        rows_from_smem<NP>(cp, Cm, lane);
+        pixel_solve<T, NP>(P, pp, sm, lane, npix, cp);
+    } else {
+        const CRowsSmem<T, NP> cp{const_cast<C2<T> *>(Cm), lane};
         pixel_solve<T, NP>(P, pp, sm, lane, npix, cp);
     }
 }

@@ -124,6 +124,23 @@ def test_fp64_form_matches_oracle_tightly(gpu_lib, vor30):
     ctx.close()
 
 
+def test_fp64_form_64_dates_matches_oracle(gpu_lib):
+    """The FP64 form at 64 dates keeps C in tensor memory (two warps per SM);
+    every pixel of an ill-conditioned scene takes it."""
+    from fringe_gb300 import _lib, phase_link
+    stack, nmap = synth.scene("illcond", 20, 24, 64, 5, 10, seed=1003)
+    ctx = _lib.Context(0)
+    ctx.set_tuning(force_fp64=True)
+    for method, sem in (("MLE", "evd"), ("EVD", "evd"), ("STBAS", "evd"), ("MLE", "phase_link")):
+        extra = {"band_width": 9} if method == "STBAS" else {}
+        g = phase_link(stack, nmap, (5, 10), method=method, semantics=sem, ctx=ctx, want_status=True, **extra)
+        o = oracle.run(stack, nmap, 5, 10, method=method, semantics=sem, **extra)
+        m = compare(g, o)
+        assert m["valid_both"] > 100, m
+        assert_parity(m, phase_tol=1e-5, tcorr_tol=1e-5)
+    ctx.close()
+
+
 @pytest.mark.parametrize("shift,backoff", [(1.5, 0.97), (1.5, 1.5)])
 def test_mle_fallback_paths(gpu_lib, vor30, shift, backoff):
     """A first shift above lambda_1 makes the Cholesky of M - sigma I fail:
