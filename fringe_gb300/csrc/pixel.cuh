@@ -505,18 +505,17 @@ __device__ bool warp_chol_c2(C2<float> *A, int n, C2<float> *col, int lane)
         __syncwarp();
         if (b2) {
             // a_ik -= l1_i conj(l1_k) + l2_i conj(l2_k), k in (j+1, i]
-            for (int k0 = (j + 2) & ~3; k0 <= i; k0 += 4) {
-                const float4 a01 = *reinterpret_cast<const float4 *>(cA + k0);
-                const float4 a23 = *reinterpret_cast<const float4 *>(cA + k0 + 2);
-                const float4 c01 = *reinterpret_cast<const float4 *>(cB + k0);
-                const float4 c23 = *reinterpret_cast<const float4 *>(cB + k0 + 2);
-                const float la[8] = {a01.x, a01.y, a01.z, a01.w, a23.x, a23.y, a23.z, a23.w};
-                const float lb[8] = {c01.x, c01.y, c01.z, c01.w, c23.x, c23.y, c23.z, c23.w};
-                C2<float> x[4];
+            // two entries per step (j is even, so k0 starts at j + 2)
+            for (int k0 = j + 2; k0 <= i; k0 += 2) {
+                const float4 a0 = *reinterpret_cast<const float4 *>(cA + k0);
+                const float4 c0 = *reinterpret_cast<const float4 *>(cB + k0);
+                const float la[4] = {a0.x, a0.y, a0.z, a0.w};
+                const float lb[4] = {c0.x, c0.y, c0.z, c0.w};
+                C2<float> x[2];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) x[u] = Ai[k0 + u];
+                for (int u = 0; u < 2; ++u) x[u] = Ai[k0 + u];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < 2; ++u) {
                     const float ax = la[2 * u], ay = la[2 * u + 1], bx = lb[2 * u], by = lb[2 * u + 1];
                     x[u].x = fmaf(-l1.x, ax, x[u].x);
                     x[u].x = fmaf(-l1.y, ay, x[u].x);
@@ -528,8 +527,7 @@ __device__ bool warp_chol_c2(C2<float> *A, int n, C2<float> *col, int lane)
                     x[u].y = fmaf(l2.x, by, x[u].y);
                 }
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    if (k0 + u > j + 1) Ai[k0 + u] = x[u];
+                for (int u = 0; u < 2; ++u) Ai[k0 + u] = x[u];
             }
         }
         __syncwarp();
@@ -583,7 +581,7 @@ __device__ void warp_chol_solve(const C2<T> *L, int n, T d0, T d1, C2<T> &b0, C2
     const C2<T> *L0 = L + lane * LD;
     const C2<T> *L1 = L + (lane + 32) * LD;
     // forward: L y = b
-#pragma unroll 4
+#pragma unroll 2
     for (int j = 0; j < n; ++j) {
         C2<T> s = (NP <= 32 || j < 32) ? cscale(b0, d0) : cscale(b1, d1);
         C2<T> y;
@@ -595,7 +593,7 @@ __device__ void warp_chol_solve(const C2<T> *L, int n, T d0, T d1, C2<T> &b0, C2
     b0 = cscale(b0, d0);
     if (NP > 32) b1 = cscale(b1, d1);
     // backward: L^H x = y, b_i -= conj(L_ji) x_j
-#pragma unroll 4
+#pragma unroll 2
     for (int j = n - 1; j >= 0; --j) {
         C2<T> s = (NP <= 32 || j < 32) ? cscale(b0, d0) : cscale(b1, d1);
         C2<T> x;
