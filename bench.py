@@ -52,8 +52,8 @@ METRIC = "phase-linked px/s (N=30, 11x21)"
 
 # what the ncu captures under profiles/ show for each kernel
 BOUND_NOTES = {
-    "solve": "instruction issue: 71% issue-active at 20 warps/SM, 22.3k warp instructions per pixel "
-             "(per-pixel FP32 factorisations and triangular solves; shared-memory pipe 65%); DRAM 1.5%, "
+    "solve": "instruction issue: 70% issue-active at 20 warps/SM, 20.7k warp instructions per pixel "
+             "(per-pixel FP32 factorisations and triangular solves; shared-memory pipe 64%); DRAM 1.5%, "
              "tensor pipe 0%",
     "gram": "operand build on the CUDA cores with 8 warps/SM: tensor pipe 17.4% active, issue 35%",
     "fp32": "per-pixel FP32 gather, Gamma and eigen-solves: latency/issue-bound with 8-11 warps/SM",
