@@ -202,6 +202,14 @@ template <> struct Lay<double, 64> {
     static constexpr size_t bytes = bytes_noc;
 };
 
+// while Gamma is summed the gather staging, the coherence and the vectors
+// (1/sqrt(P) among them) are all live, so they must not overlap; the work
+// matrix may overlap the coherence (it is used only after C moved out)
+static_assert(Lay<double, 64>::cm >= Lay<double, 64>::wm + Lay<double, 64>::stage, "staging overlaps C");
+static_assert(Lay<double, 64>::vv >= Lay<double, 64>::cm + Lay<double, 64>::mat, "vectors overlap C");
+static_assert(Lay<double, 64>::vv >= Lay<double, 64>::wm + Lay<double, 64>::wm_bytes, "vectors overlap W");
+static_assert(2 * Lay<double, 64>::bytes <= 224 * 1024, "two warps per CTA");
+
 // kernels whose warps hold C in tensor memory in the FP64 form
 template <typename T, int NP> struct CInTmem {
     static constexpr bool value = sizeof(T) == 8 && NP == 64;
