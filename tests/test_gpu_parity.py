@@ -56,6 +56,31 @@ def test_uniform_n10(gpu_lib, method):
     assert_parity(m)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+@pytest.mark.parametrize("method", ["EVD", "MLE"])
+def test_cpu_runnable_configuration_full_scene(gpu_lib, method, precision):
+    """The CPU-runnable configuration at its full size: 200x200 pixels,
+    N = 10, half-window 5x5, all-ones SHP map (edge-clipped windows at the
+    borders); every pixel valid in both."""
+    stack, nmap = synth.scene("uniform", 200, 200, 10, 5, 5, seed=1001)
+    g, o = _run_both(stack, nmap, 5, 5, method=method, precision=precision)
+    m = compare(g, o)
+    assert m["valid_both"] == 200 * 200, m
+    assert_parity(m)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_ill_conditioned_64_dates_tile(gpu_lib, precision):
+    """A tile of the ill-conditioned 64-date configuration (per-pixel
+    coherence U(0.05, 0.9), decorrelated pixels): MLE through the FP32 band
+    and the FP64 settle."""
+    stack, nmap = synth.scene("illcond", 48, 64, 64, 5, 10, seed=1003)
+    g, o = _run_both(stack, nmap, 5, 10, method="MLE", precision=precision)
+    m = compare(g, o)
+    assert m["valid_both"] > 1000, m
+    assert_parity(m)
+
+
 @pytest.mark.parametrize("nb", [1, 2, 3, 15, 16, 17, 31, 32, 33, 47, 63, 64])
 def test_depths(gpu_lib, nb):
     stack, nmap = synth.scene("voronoi", 20, 24, nb, 2, 3, seed=100 + nb)
