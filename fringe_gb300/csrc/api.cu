@@ -391,13 +391,33 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job)
         float *d_tcorr = static_cast<float *>(ctx->d_tcorr);
         int32_t *d_status = job->status ? static_cast<int32_t *>(ctx->d_status) : nullptr;
         const char *h_stack = static_cast<const char *>(job->stack);
-        int step = (r1 - r0 + kRunChunks - 1) / kRunChunks;
-        step = std::max(8, (step + 7) & ~7);
-        nchunks = std::max(1, (r1 - r0 + step - 1) / step);
+        // chunk c computes rows [cb[c], cb[c+1]).  The first chunk's upload
+        // and the last chunk's download overlap no compute, so those chunks
+        // are the smallest (row shares 1,2,3,..,3,2,1, multiples of 8
+        // rows); short ranges are cut into equal chunks of >= 8 rows.
+        int cb[kRunChunks + 1];
+        {
+            static_assert(kRunChunks == 8, "chunk weights");
+            const int wsum[kRunChunks + 1] = {0, 1, 3, 6, 9, 12, 15, 17, 18};
+            const int span = r1 - r0;
+            cb[0] = r0;
+            nchunks = 0;
+            if (span >= 8 * 18) {
+                for (int c = 1; c <= kRunChunks; ++c)
+                    cb[c] = (c == kRunChunks) ? r1 : r0 + (int)((long long)span * wsum[c] / 18) / 8 * 8;
+                nchunks = kRunChunks;
+            } else {
+                int step = (span + kRunChunks - 1) / kRunChunks;
+                step = std::max(8, (step + 7) & ~7);
+                for (int a = r0; a < r1; a += step) cb[++nchunks] = std::min(r1, a + step);
+            }
+            nchunks = std::max(nchunks, 1);
+            if (span <= 0) cb[1] = r1;
+        }
         int copied = std::max(0, r0 / 8 * 8 - ny);     // first stack row on the device
         FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
         for (int c = 0; c < nchunks; ++c) {
-            const int a = r0 + c * step, b = std::min(r1, a + step);
+            const int a = cb[c], b = cb[c + 1];
             if (b <= a) continue;
             // stack rows every computed pixel's window (and the chunk's tiles) read
             const int need = std::min(rows, (b + 7) / 8 * 8 + ny);
