@@ -174,6 +174,31 @@ def cpu_baseline(stack, nmap, method, rows):
                       % (rows, stack.shape[1], stack.shape[2], px, method, dt)}
 
 
+def cpu_baseline_detail(stack, nmap, rows):
+    """Oracle port on the host cores for both methods: the CPU-runnable
+    configuration in full (200x200, N = 10, half-window 5x5, all-ones SHP
+    map) in EVD and MLE, and EVD over rows [0, rows) of the headline scene
+    (its MLE sample is the main cpu_baseline).  A few seconds in all."""
+    import oracle
+    from fringe_gb300 import synth
+    threads = os.cpu_count() or 1
+    res = {"cores": threads, "kind": "port"}
+    st1, nm1 = synth.scene("uniform", 200, 200, 10, 5, 5, seed=1001)
+    for method in ("EVD", "MLE"):
+        t0 = time.perf_counter()
+        oracle.run(st1, nm1, 5, 5, method=method, nthreads=threads)
+        dt = time.perf_counter() - t0
+        res["uniform200_n10_%s" % method.lower()] = {"value": 200 * 200 / dt, "unit": "px/s",
+                                                     "sample": "whole 200x200 scene, %.2f s" % dt}
+    t0 = time.perf_counter()
+    oracle.run(stack, nmap, NY, NX, method="EVD", rows=(0, rows), nthreads=threads)
+    dt = time.perf_counter() - t0
+    res["voronoi_n30_evd"] = {"value": rows * stack.shape[2] / dt, "unit": "px/s",
+                              "sample": "rows 0..%d of the %dx%d scene, %.1f s" % (rows, stack.shape[1],
+                                                                                    stack.shape[2], dt)}
+    return res
+
+
 def serving_measurement(njobs, seed=5):
     """Serving loop on a mix of jobs: tiles 256^2..1024^2, N in 10..60,
     half-windows 3x3..5x10, MLE/EVD, in the mixed-precision form and in the
@@ -677,6 +702,7 @@ def main():
     if not args.no_cpu:
         rows = args.cpu_rows or 480          # about 15 s on 16 host cores
         line["cpu_baseline"] = cpu_baseline(stack, nmap, args.method, min(rows, R))
+        line["cpu_baseline_detail"] = cpu_baseline_detail(stack, nmap, min(rows // 4, R))
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
