@@ -44,6 +44,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# LAPACK single-threaded inside the OpenMP pixel loop, as the reference's
+# module scripts set it (src/evd/evd.py:43)
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
 
 NB, ROWS, COLS, NY, NX = 30, 2048, 2048, 5, 10
 SEED = 1002
@@ -162,16 +165,37 @@ class ClockSampler:
 
 
 def cpu_baseline(stack, nmap, method, rows):
-    """Oracle port on the host cores over rows [0, rows) of the scene."""
+    """Oracle port on the host cores over rows [0, rows) of the scene; also
+    returns the oracle's result for those rows (the parity check)."""
     import oracle
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    oracle.run(stack, nmap, NY, NX, method=method, rows=(0, rows), nthreads=threads)
+    res = oracle.run(stack, nmap, NY, NX, method=method, rows=(0, rows), nthreads=threads)
     dt = time.perf_counter() - t0
     px = rows * stack.shape[2]
     return {"value": px / dt, "unit": "px/s", "cores": threads, "kind": "port",
             "sample": "rows 0..%d of the %dx%d scene (%d px), %s, evd semantics, %.1f s"
-                      % (rows, stack.shape[1], stack.shape[2], px, method, dt)}
+                      % (rows, stack.shape[1], stack.shape[2], px, method, dt)}, res
+
+
+def parity_vs_oracle(gpu_out, ora, rows, tol):
+    """Parity of one GPU form against the oracle over rows [0, rows) of the
+    same scene: phase RMS / max (wrapped, over pixels valid in both), max
+    |dtcorr|, validity-code mismatches, compressed-SLC error (in units of the
+    oracle's mean |comp|) and whether each is within the stated tolerance."""
+    sys.path.insert(0, ROOT)
+    from tests.parity import COMP_RMS_TOL, compare
+    g = {k: gpu_out[k][..., :rows, :].cpu().numpy() for k in ("phase", "tcorr", "comp")}
+    o = {k: ora[k][..., :rows, :] for k in ("phase", "tcorr", "comp")}
+    m = compare(g, o)
+    tol = dict(tol, comp_rms=min(tol["phase_rms"], COMP_RMS_TOL))
+    ok = (m["code_mismatch"] == 0 and m["phase_rms"] <= tol["phase_rms"] and m["tcorr_max"] <= tol["tcorr_max"]
+          and m["comp_rms"] <= tol["comp_rms"] and m["zero_mismatch"] == 0 and m["comp_zero_mismatch"] == 0)
+    return {"pixels_compared": m["valid_both"], "rows": "0..%d" % rows, "phase_rms_rad": m["phase_rms"],
+            "phase_max_rad": m["phase_max"], "tcorr_max_abs": m["tcorr_max"],
+            "code_mismatch_px": m["code_mismatch"], "comp_rms": m["comp_rms"], "comp_max": m["comp_max"],
+            "skipped_not_zero_px": m["zero_mismatch"] + m["comp_zero_mismatch"],
+            "tolerance": tol, "within_tolerance": bool(ok)}
 
 
 def cpu_baseline_detail(stack, nmap, rows):
@@ -200,15 +224,16 @@ def cpu_baseline_detail(stack, nmap, rows):
 
 
 def serving_measurement(njobs, seed=5):
-    """Serving loop on a mix of jobs: tiles 256^2..1024^2, N in 10..60,
+    """Serving loop on a mix of jobs: tiles 256^2..2048^2, N in 10..60,
     half-windows 3x3..5x10, MLE/EVD, in the mixed-precision form and in the
     plain FP32 form.  Per form: (1) all jobs submitted at once (saturating
     load): throughput and p50/p99 latency; (2) Poisson arrivals at 30, 50, 70
-    and 90% of the saturated job rate: p50/p99 latency."""
+    and 90% of the saturated job rate: p50/p99 latency, overall and per tile
+    size."""
     from fringe_gb300 import synth
     from fringe_gb300.serve import Server
     shapes = [(256, 10, (3, 3)), (512, 30, (5, 10)), (1024, 20, (3, 5)), (512, 60, (5, 10)),
-              (256, 45, (4, 8)), (1024, 30, (5, 10))]
+              (256, 45, (4, 8)), (1024, 30, (5, 10)), (2048, 30, (5, 10)), (2048, 15, (3, 3))]
     import torch
 
     def pinned(a):
@@ -226,7 +251,16 @@ def serving_measurement(njobs, seed=5):
                 "comp": torch.zeros((R, C), dtype=torch.complex64).pin_memory().numpy()}
 
     result = {"jobs": int(njobs),
-              "mix": "tiles 256^2..1024^2, N 10..60, half-windows 3x3..5x10, MLE/EVD, 80 GB budget"}
+              "mix": "tiles 256^2..2048^2, N 10..60, half-windows 3x3..5x10, MLE/EVD, 80 GB budget"}
+
+    def by_size(picks, lat):
+        out = {}
+        for size in sorted({pool[p][0].shape[1] for p in picks}):
+            sel = np.array([pool[p][0].shape[1] == size for p in picks])
+            out["%dx%d" % (size, size)] = {"jobs": int(sel.sum()),
+                                           "p50_ms": float(np.percentile(lat[sel], 50)),
+                                           "p99_ms": float(np.percentile(lat[sel], 99))}
+        return out
     for prec in ("mixed", "fp32"):
         rng = np.random.Generator(np.random.PCG64(seed))
         picks = rng.integers(0, len(pool), njobs)
@@ -262,31 +296,43 @@ def serving_measurement(njobs, seed=5):
             arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs))
             w, lat_p = run(arrivals)
             sweep.append({"load": frac, "rate_jobs_per_s": rate, "throughput_px_s": px / w,
-                          "p50_ms": float(np.percentile(lat_p, 50)), "p99_ms": float(np.percentile(lat_p, 99))})
+                          "p50_ms": float(np.percentile(lat_p, 50)), "p99_ms": float(np.percentile(lat_p, 99)),
+                          "by_tile": by_size(picks, lat_p)})
         srv.close()
         result["pixels"] = px
         result[prec] = {
             "saturated": {"throughput_px_s": px / wall, "jobs_per_s": rate_sat,
-                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
+                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                          "by_tile": by_size(picks, lat)},
             "poisson": sweep}
     return result
 
 
 def run_reference(args, rank):
+    """The reference's CPU implementation of the path on the host cores: the
+    oracle loop linked to the reference's own EVWorker + LAPACK where that
+    build exists (oracle/_ref), else the oracle port; each step phase-links
+    a band of rows of the same scene (rank 0 only)."""
     if rank != 0:
         return
     from fringe_gb300 import synth
     stack, nmap = synth.scene("voronoi", args.rows, args.cols, NB, NY, NX, seed=SEED)
     import oracle
+    kind = "port"
+    try:
+        oracle.load("reference")
+        kind = "reference"
+    except (FileNotFoundError, OSError):
+        pass
     threads = os.cpu_count() or 1
     rows = args.cpu_rows or 16
     rows = min(rows, args.rows)
     for _ in range(args.warmup):
-        oracle.run(stack, nmap, NY, NX, method=args.method, rows=(0, 2), nthreads=threads)
+        oracle.run(stack, nmap, NY, NX, method=args.method, rows=(0, 2), nthreads=threads, kind=kind)
     t0 = time.perf_counter()
     for s in range(args.steps):
         r0 = (s * rows) % max(1, args.rows - rows)
-        oracle.run(stack, nmap, NY, NX, method=args.method, rows=(r0, r0 + rows), nthreads=threads)
+        oracle.run(stack, nmap, NY, NX, method=args.method, rows=(r0, r0 + rows), nthreads=threads, kind=kind)
     dt = time.perf_counter() - t0
     px = args.steps * rows * args.cols
     v = px / dt
@@ -295,14 +341,17 @@ def run_reference(args, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "voronoi %dx%d N=%d half-window %dx%d %s"
-                               % (args.rows, args.cols, NB, NY, NX, args.method),
+        "config": {"workload": workload_name(args.rows, args.cols, args.method),
                    "sample_rows_per_step": rows},
-        "cpu_baseline": {"value": v, "unit": "px/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": "px/s", "cores": threads, "kind": kind,
                          "sample": "%d rows x %d cols per step" % (rows, args.cols)},
         "e2e": {"value": v, "unit": "px/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def workload_name(rows, cols, method):
+    return "voronoi %dx%d N=%d half-window %dx%d %s evd-semantics" % (rows, cols, NB, NY, NX, method)
 
 
 def device_form(phase_link, d_stack, d_nmap, ctx, precision, method, steps, warmup, dist, local):
@@ -478,39 +527,56 @@ def batch_measurement(stack, nmap, seed=7):
     return res
 
 
-def illcond_measurement(ctx):
+def illcond_measurement(ctx, cpu_rows=24, size=1024):
     """Ill-conditioned MLE stress (gamma0 ~ U(0.05, 0.9), 10% of pixels with
-    gamma_inf = 0): N = 64, 512^2 pixels (a sub-scene of the 1024^2
-    configuration), half-window 5x10: px/s and error of the mixed form
-    against the FP64 form, and the share of pixels settled in FP64."""
+    gamma_inf = 0): N = 64, the configuration's full 1024^2 pixels,
+    half-window 5x10: px/s of the mixed form, the share of pixels settled in
+    FP64, its error against the FP64 form over the whole scene, and parity of
+    both forms against the oracle over a row sample."""
     import torch
     from fringe_gb300 import phase_link, synth
-    st, nm = synth.scene("illcond", 512, 512, 64, NY, NX, seed=1003)
+    st, nm = synth.scene("illcond", size, size, 64, NY, NX, seed=1003)
     d, dn = torch.from_numpy(st).cuda(), torch.from_numpy(nm.view(np.int32)).cuda()
-    out = None
-    for _ in range(2):
-        out = phase_link(d, dn, (NY, NX), method="MLE", precision="mixed", ctx=ctx, out=out)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(3):
-        phase_link(d, dn, (NY, NX), method="MLE", precision="mixed", ctx=ctx, out=out)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / 3
-    # fp64-settled count of one run on the context's stream
-    h = phase_link(st, nm, (NY, NX), method="MLE", precision="mixed", ctx=ctx)
-    fp64_px = ctx.stats()["fp64_pixels"]
-    ref = {k: torch.zeros_like(v) for k, v in out.items()}
+    res = {"workload": "illcond %dx%d N=64 half-window 5x10 MLE evd-semantics" % (size, size)}
+    outs = {}
+    for prec in ("mixed", "fp32"):
+        # one host-memory run (synchronous fpl_run) for the FP64-settled count
+        phase_link(st, nm, (NY, NX), method="MLE", precision=prec, ctx=ctx)
+        fp64_px = ctx.stats()["fp64_pixels"]
+        out = None
+        for _ in range(2):
+            out = phase_link(d, dn, (NY, NX), method="MLE", precision=prec, ctx=ctx, out=out)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            phase_link(d, dn, (NY, NX), method="MLE", precision=prec, ctx=ctx, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+        outs[prec] = out
+        res[prec] = {"value": size * size / ms * 1e3, "unit": "px/s", "ms": ms,
+                     "fp64_settled_px": int(fp64_px), "fp64_settled_share": fp64_px / float(size * size)}
+    ref = {k: torch.zeros_like(v) for k, v in outs["mixed"].items()}
     ctx.set_tuning(force_fp64=True)
     phase_link(d, dn, (NY, NX), method="MLE", ctx=ctx, out=ref)
     torch.cuda.synchronize()
     ctx.set_tuning(force_fp64=False)
-    acc = accuracy(out, ref, ref["tcorr"] > 0)
-    return {"workload": "illcond 512x512 N=64 half-window 5x10 MLE (mixed form)",
-            "value": 512 * 512 / ms * 1e3, "unit": "px/s", "ms": ms,
-            "fp64_settled_px": int(fp64_px), "accuracy_vs_fp64": acc}
+    for prec in ("mixed", "fp32"):
+        res[prec]["accuracy_vs_fp64"] = accuracy(outs[prec], ref, ref["tcorr"] > 0)
+    del ref
+    if cpu_rows:
+        import oracle
+        t0 = time.perf_counter()
+        ora = oracle.run(st, nm, NY, NX, method="MLE", rows=(0, cpu_rows), nthreads=os.cpu_count() or 1)
+        dt = time.perf_counter() - t0
+        tol = {"phase_rms": 1e-3, "tcorr_max": 2e-4}
+        res["parity_vs_oracle"] = {p: parity_vs_oracle(outs[p], ora, cpu_rows, tol) for p in ("mixed", "fp32")}
+        res["cpu_baseline"] = {"value": cpu_rows * size / dt, "unit": "px/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": "rows 0..%d (%.1f s)" % (cpu_rows, dt)}
+    res["value"] = res["mixed"]["value"]
+    return res
 
 
 def accuracy(out, ref, valid_ref):
@@ -666,8 +732,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == "fp32" else "bf16x2-split/f32",
         "data": "synthetic (seeded Voronoi scene, coherence model of tests/evd/test_evd.py)",
-        "config": {"workload": "voronoi %dx%d N=%d half-window %dx%d %s evd-semantics"
-                               % (R, C, NB, NY, NX, args.method),
+        "config": {"workload": workload_name(R, C, args.method),
                    "precision": args.precision, "mean_shp": sbar,
                    "l2": "inputs (%.2f GB stack) exceed the 129 MB L2; no flush needed" % (stack.nbytes / 1e9),
                    "valid_px": valid, "fp64_settled_px": fp64_px},
@@ -695,13 +760,17 @@ def main():
         line["serving"] = serving_measurement(args.serve_jobs)
     if not args.no_batch and world == 1:
         line["batch"] = batch_measurement(stack, nmap)
-        line["illconditioned"] = illcond_measurement(ctx)
+        line["illconditioned"] = illcond_measurement(ctx, 0 if args.no_cpu else 24)
     if not args.no_nmap and world == 1:
         line["nmap"] = nmap_measurement(stack, d_stack, ctx, max(1, args.steps), 0 if args.no_cpu else 384)
         line["integrate_ps"] = integrate_ps_measurement(d_stack, ctx, max(3, args.steps), hbm_peak)
     if not args.no_cpu:
-        rows = args.cpu_rows or 480          # about 15 s on 16 host cores
-        line["cpu_baseline"] = cpu_baseline(stack, nmap, args.method, min(rows, R))
+        rows = min(args.cpu_rows or 480, R)          # about 15 s on 16 host cores
+        line["cpu_baseline"], ora = cpu_baseline(stack, nmap, args.method, rows)
+        tols = {"fp32": {"phase_rms": 1e-3, "tcorr_max": 1e-4}, "mixed": {"phase_rms": 1e-3, "tcorr_max": 2e-4}}
+        line["parity_vs_oracle"] = {p: parity_vs_oracle(outs[p], ora, rows, tols[p]) for p in forms}
+        line["parity_vs_oracle"]["oracle"] = "oracle port (FP64 restatement of the reference loop), same scene"
+        del ora
         line["cpu_baseline_detail"] = cpu_baseline_detail(stack, nmap, min(rows // 4, R))
     print(json.dumps(line), flush=True)
     if dist:

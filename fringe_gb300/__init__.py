@@ -10,8 +10,10 @@ temporal coherence) runs as CUDA kernels behind the C ABI declared in
   module, two-sample KS test) that phase linking consumes;
 * ``integrate_ps(ds, slc, tcorr, ps)`` -- the PS/DS merge of the
   integratePS workflow step (single-master interferograms, PS coherence);
-* ``evdlib.Evd`` / ``phase_linklib.Phaselink`` -- drop-in replacements of the
-  reference's module wrappers (file level);
+* ``fringe_gb300.evdlib.Evd`` / ``fringe_gb300.evdlib.Phaselink`` -- drop-in
+  replacements of the reference's module wrappers (file level), re-exported
+  under the reference's module names by the top-level modules ``evdlib`` and
+  ``phase_linklib`` at the repository root;
 * ``synth`` -- seeded synthetic stacks and SHP bitmasks.
 """
 from .linker import integrate_ps, nmap, phase_link  # noqa: F401

@@ -15,6 +15,25 @@ FPL_SEMANTICS = {"evd": 0, "phase_link": 1}
 FPL_PRECISION = {"fp32": 0, "mixed": 1}
 FPL_MEM_HOST, FPL_MEM_DEVICE = 0, 1
 FPL_BATCH_GRAPH, FPL_BATCH_AUTOTUNE = 1, 2
+HEADER = os.path.join(os.path.dirname(HERE), "include", "fringe_gb300.h")
+
+
+def header_defines(path=HEADER):
+    """Integer #define constants of the C header, read from the header itself
+    so that Python callers and tests cannot drift from it."""
+    out = {}
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == "#define":
+                try:
+                    out[parts[1]] = int(parts[2], 0)
+                except ValueError:
+                    pass
+    return out
+
+
+FPL_NOALLOC_MAX_PIXELS = header_defines()["FPL_NOALLOC_MAX_PIXELS"]
 
 
 class FplJob(ctypes.Structure):

@@ -20,6 +20,9 @@
 // All calls share the one array and each call leaves its contents behind:
 // the counters are cleared on the caller's stream at the start of every
 // call, and two calls whose work overlaps on the GPU race on the array.
+// A call reports no statistics and no device error flags: the one flag the
+// kernels raise (FP64 work list full) cannot be set here, because the list
+// holds an entry for every pixel a call may cover.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -39,24 +42,29 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kCounterBytes +
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
 int g_num_sms[kMaxDevices] = {};
 
-// Once per device, with that device current: the device address of the
-// scratch array (host code cannot use the symbol itself as an address).
+// With the caller's device current: the device address of the scratch array
+// in the current CUDA context (host code cannot use the symbol itself as an
+// address).  The address is looked up on every call, not cached: it belongs
+// to the context that is current, and a cudaDeviceReset or a caller working
+// through its own driver context loads the library's module again, possibly
+// at another address.  Once the module is loaded in a context the lookup is
+// a table read; the first call in a context loads it.  The SM count is a
+// property of the device and is cached.
 int noalloc_setup(int dev, unsigned char **addr, int *sms)
 {
     if (dev < 0 || dev >= kMaxDevices) return FPL_ERR_UNSUPPORTED;
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FPL_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FPL_ERR_CUDA;
+    if (!g_num_sms[dev]) {
         int n = 0;
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FPL_ERR_CUDA;
-        g_scratch_addr[dev] = p;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            return FPL_ERR_CUDA;
         g_num_sms[dev] = n;
     }
-    *addr = static_cast<unsigned char *>(g_scratch_addr[dev]);
+    *addr = static_cast<unsigned char *>(p);
     *sms = g_num_sms[dev];
     return FPL_OK;
 }

@@ -6,8 +6,11 @@ src/phase_link/phase_linklib.pyx:33-157): the same property names and
 defaults (src/evd/evd.hpp:58-68), ``print()`` and ``run()``.  ``run()`` calls
 ``fpl_process`` in libfringe_gb300.so and returns its code (0, or the
 reference's module codes 101-121; the reference's wrappers discard it).
+The top-level modules ``evdlib`` and ``phase_linklib`` at the repository root
+re-export these classes under the reference's module names.
 """
 import ctypes
+import os
 
 from . import _lib
 
@@ -42,7 +45,9 @@ class _Module:
         # evdOptions leaves the compressed-SLC names empty; the scripts set them
         self._v["outputCompressedSlcFolder"] = ""
         self._v["compSlc"] = ""
-        self.precision = "fp32"
+        self.precision = os.environ.get("FRINGE_GB300_PRECISION", "fp32")
+        if self.precision not in _lib.FPL_PRECISION:
+            raise ValueError("FRINGE_GB300_PRECISION must be one of %s" % sorted(_lib.FPL_PRECISION))
         self.device = 0
         self.verbose = 1
 

@@ -210,12 +210,18 @@ int fpl_server_destroy(fpl_server *srv);
  * here: the mixed form's coherence records need gigabytes of scratch), on
  * the current CUDA device, but no context is needed and nothing is
  * allocated: the kernels' scratch is a fixed array inside the library, held
- * by every GPU that loads it until the process exits.  The first call on a
- * device looks up that array's device address; make that first call before
- * any stream capture.  A call covers at most FPL_NOALLOC_MAX_PIXELS pixels
- * ((row_end - row_begin) * cols); larger jobs return FPL_ERR_NOALLOC_LIMIT and
- * can be split into row ranges.  All calls share the array, so calls whose
- * work overlaps on the GPU race; serialise them on one stream. */
+ * by every GPU that loads it until the process exits.  Every call looks up
+ * that array's device address in the current CUDA context; the first call
+ * in a context (on a device, after a cudaDeviceReset, or in a driver context
+ * of the caller's) also loads the library's module there, so make that
+ * first call before any stream capture.  A call covers at most
+ * FPL_NOALLOC_MAX_PIXELS pixels ((row_end - row_begin) * cols); larger jobs
+ * return FPL_ERR_NOALLOC_LIMIT and can be split into row ranges, which give
+ * the same results bit for bit.  All calls share the array, so calls whose
+ * work overlaps on the GPU race; serialise them on one stream.  A call
+ * reports no statistics and no device error flags (the kernels' one flag,
+ * FP64 work list full, cannot be raised: the list has an entry for every
+ * pixel a call may cover). */
 #define FPL_NOALLOC_MAX_PIXELS 524288
 int fpl_run_noalloc(const fpl_job *job, void *stream);
 

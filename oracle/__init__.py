@@ -47,11 +47,24 @@ def build_port(force=False):
     return PORT_SO
 
 
-def build_reference(reference_root="/root/reference"):
-    """Compile oracle/_ref/libfpl_ref.so; returns its path or None."""
-    r = subprocess.run([os.path.join(HERE, "build_ref.sh"), reference_root],
-                       capture_output=True, text=True)
+def build_reference(reference_root=None):
+    """Compile oracle/_ref/libfpl_ref.so; returns its path or None.
+
+    reference_root: the reference source tree; default the environment
+    variable FRINGE_REFERENCE_ROOT, else build_ref.sh's own default.  Where
+    the tree is absent the recipe exits without building (None here)."""
+    root = reference_root or os.environ.get("FRINGE_REFERENCE_ROOT")
+    cmd = [os.path.join(HERE, "build_ref.sh")] + ([root] if root else [])
+    r = subprocess.run(cmd, capture_output=True, text=True)
     return REF_SO if r.returncode == 0 and os.path.exists(REF_SO) else None
+
+
+def reference_root():
+    """The reference source tree the recipes use (FRINGE_REFERENCE_ROOT, else
+    build_ref.sh's default), or None where it is absent (a GPU host)."""
+    r = subprocess.run([os.path.join(HERE, "build_ref.sh"), "--root"], capture_output=True, text=True)
+    root = r.stdout.strip()
+    return root if root and os.path.isfile(os.path.join(root, "include", "fringe", "EigenLapack.hpp")) else None
 
 
 _LIBS = {}

@@ -4,9 +4,14 @@
 # reference tree where it lies, with LAPACK taken from SciPy's bundled
 # OpenBLAS (its symbols carry a "scipy_" prefix).  Test infrastructure only.
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#        oracle/build_ref.sh --root     (prints the reference tree it would use)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${1:-/root/reference}
+if [ "$1" = "--root" ]; then
+    echo "${FRINGE_REFERENCE_ROOT:-/root/reference}"
+    exit 0
+fi
+REF=${1:-${FRINGE_REFERENCE_ROOT:-/root/reference}}
 if [ ! -f "$REF/include/fringe/EigenLapack.hpp" ]; then
     echo "build_ref: reference headers not found under $REF; skipping" >&2
     exit 3

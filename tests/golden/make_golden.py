@@ -5,6 +5,8 @@ the reference's own EVWorker, include/fringe/EigenLapack.hpp, and LAPACK).
 
 Run where the reference tree is present:
     OPENBLAS_NUM_THREADS=1 python tests/golden/make_golden.py [REFERENCE_ROOT]
+(REFERENCE_ROOT defaults to $FRINGE_REFERENCE_ROOT, else to the default of
+oracle/build_ref.sh.)
 Inputs (seeded synthetic scenes from fringe_gb300.synth) are stored with the
 outputs, so the fixtures do not depend on the generator's reproducibility.
 Phases are stored as float32 angles.
@@ -41,7 +43,7 @@ def variant_key(case, method, sem, extra):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else None     # else FRINGE_REFERENCE_ROOT
     if not oracle.build_reference(ref_root):
         sys.exit("reference build of the oracle is unavailable")
     out = {}

@@ -8,7 +8,8 @@ these two functions, which only call ReadAsArray / GetRasterBand /
 WriteArray on the datasets they are given.  The script registers empty
 stand-ins for those modules and passes in-memory datasets with the same
 methods.  Run where the reference tree is present:
-    python tests/golden/make_ps_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_ps_golden.py REFERENCE_ROOT
+(or with FRINGE_REFERENCE_ROOT set).
 """
 import os
 import sys
@@ -17,7 +18,9 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FRINGE_REFERENCE_ROOT")
+if not REF:
+    sys.exit("usage: make_ps_golden.py REFERENCE_ROOT (or set FRINGE_REFERENCE_ROOT)")
 
 
 class _Band:

@@ -108,6 +108,7 @@ def test_reference_build_matches_golden_when_available(golden):
                      kind="reference", **extra)
     m = compare(got, ref)
     assert m["code_mismatch"] == 0 and m["phase_max"] < 1e-6
+    assert m["comp_max"] == 0.0 and m["comp_zero_mismatch"] == 0, m
 
 
 def test_row_ranges_are_block_invariant():
