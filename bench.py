@@ -54,13 +54,29 @@ METRIC = "phase-linked px/s (N=30, 11x21)"
 
 
 # what the ncu captures under profiles/ show for each kernel
+# what the ncu captures under profiles/ show for each kernel
 BOUND_NOTES = {
-    "solve": "instruction issue: 70% issue-active at 20 warps/SM, 20.7k warp instructions per pixel "
-             "(per-pixel FP32 factorisations and triangular solves; shared-memory pipe 64%); DRAM 1.5%, "
-             "tensor pipe 0%",
-    "gram": "operand build on the CUDA cores with 8 warps/SM: tensor pipe 17.4% active, issue 35%",
-    "fp32": "per-pixel FP32 gather, Gamma and eigen-solves: latency/issue-bound with 8-11 warps/SM",
+    "solve": "instruction issue (one warp per pixel; per-pixel FP32 factorisations, sweep inverse and "
+             "triangular solves); DRAM and tensor pipe idle",
+    "gram": "operand build on the CUDA cores with 8 warps/SM and a barrier per chunk; tensor pipe partly idle",
+    "fp32": "per-pixel FP32 gather, Gamma and eigen-solves: latency/issue-bound",
 }
+# FP32 flops of the MLE eigen-solves per pixel as implemented, for n dates and
+# `solves` pairs of triangular solves: the Cholesky test of C - 1e-6 I and the
+# Cholesky of M - sigma I (n^3/6 complex multiply-adds each, 8 flops), the
+# sweep inverse of the real |C| (n^3 multiply-adds, 2 flops), the start
+# vector and Rayleigh quotient (5 complex matrix-vector products) and the
+# inverse-iteration solves (n^2 complex multiply-adds per pair).
+def solve_flops_per_px(n, solves):
+    return 2 * (n ** 3 / 6.0) * 8 + n ** 3 * 2 + 5 * n * n * 8 + solves * n * n * 8
+
+
+def kernel_counters():
+    p = os.path.join(ROOT, "profiles", "kernel_counters.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
 
 
 def parse():
@@ -707,15 +723,44 @@ def main():
              "gram": "k_gram_box (tcgen05 bf16 hi/lo Gamma, TMEM accumulate)",
              "solve": "k_solve (warp eigen-solves from the Gamma records)"}
     k_ms = km[dom]
-    achieved_tf = flops / (k_ms / 1e3) / 1e12
-    traffic = None
-    tf_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf_path):
-        with open(tf_path) as f:
-            tj = json.load(f)
-        ent = tj.get(dom) if isinstance(tj.get(dom), dict) else None
-        if ent and ent.get("kernel_bytes_per_px"):
-            traffic = ent["kernel_bytes_per_px"] * npx
+    kc = kernel_counters()
+    ent = kc.get(dom) or {}
+    traffic = ent["dram_bytes_per_px"] * npx if ent.get("dram_bytes_per_px") else None
+    clk_mhz = head["clocks"].get("sm_mhz") or 2070.0
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    issue_peak = sms * 4 * clk_mhz * 1e6 / 1e9          # warp instructions per second, G
+    fp32_peak = sms * 128 * 2 * clk_mhz * 1e6 / 1e12     # FP32 FMA pipe, TFLOP/s
+    gamma_tf = flops / (km["gram"] / 1e3) / 1e12 if km.get("gram", 0) > 0 else None
+    if dom in ("solve", "fp32") and ent.get("warp_inst_per_px"):
+        inst = ent["warp_inst_per_px"] * npx / (k_ms / 1e3) / 1e9
+        sflops = float(solve_flops_per_px(NB, ent.get("solve_pairs_per_px") or 4.6)) * valid / (k_ms / 1e3) / 1e12
+        roof = {"bound": "issue", "achieved": inst, "peak": issue_peak, "unit": "Gwarp-inst/s",
+                "frac": inst / issue_peak, "traffic": traffic, "kernel": names[dom], "kernel_ms": k_ms,
+                "work": "ncu warp instructions per pixel x pixels, per step",
+                "peak_source": "%d SMs x 4 issue slots x %.0f MHz (median SM clock of the timed region)"
+                               % (sms, clk_mhz),
+                "fp32": {"achieved_tflops": sflops, "peak_tflops": fp32_peak, "frac": sflops / fp32_peak,
+                         "work": "eigen-solve FP32 flops per valid pixel as implemented (solve_flops_per_px)"},
+                "ncu": {k: ent.get(k) for k in ("issue_active", "fma_pipe_active", "tensor_pipe_active",
+                                                 "warp_inst_per_px", "dram_bytes_per_px", "source")},
+                "hbm_achieved_gbs": alg_bytes / (k_ms / 1e3) / 1e9, "hbm_peak_gbs": hbm_peak,
+                "what_bounds_it": BOUND_NOTES.get(dom, "")}
+    else:
+        achieved_tf = flops / (k_ms / 1e3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved_tf, "peak": tf_peak, "unit": "TFLOP/s",
+                "frac": achieved_tf / tf_peak, "traffic": traffic, "peak_source": peak_src,
+                "kernel": names[dom], "work": "Gamma flops 4N(N+1)S summed over pixels, per step",
+                "kernel_ms": k_ms, "what_bounds_it": BOUND_NOTES.get(dom, "")}
+    gram_line = None
+    if gamma_tf:
+        g = kc.get("gram") or {}
+        gram_line = {"bound": "tensor", "kernel": names["gram"], "kernel_ms": km["gram"],
+                     "achieved": gamma_tf, "peak": tf_peak, "unit": "TFLOP/s", "frac": gamma_tf / tf_peak,
+                     "peak_source": peak_src + " bf16 burst",
+                     "work": "Gamma flops 4N(N+1)S summed over pixels (hi/lo passes and masked-out products "
+                             "not credited)",
+                     "traffic": g["dram_bytes_per_px"] * npx if g.get("dram_bytes_per_px") else None,
+                     "ncu_tensor_pipe_active": g.get("tensor_pipe_active")}
     per_kernel = {}
     for k, v in km.items():
         if v <= 0:
@@ -739,14 +784,8 @@ def main():
         "e2e": e2e,
         "gpu_launches": head["launches_per_step"] * args.steps,
         "clocks": head["clocks"],
-        "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": tf_peak,
-                     "unit": "TFLOP/s", "frac": achieved_tf / tf_peak, "traffic": traffic,
-                     "peak_source": peak_src, "kernel": names[dom],
-                     "work": "Gamma flops 4N(N+1)S summed over pixels, per step",
-                     "kernel_ms": k_ms,
-                     "hbm_achieved_gbs": alg_bytes / (k_ms / 1e3) / 1e9,
-                     "hbm_peak_gbs": hbm_peak,
-                     "what_bounds_it": BOUND_NOTES.get(dom, "")},
+        "roofline": roof,
+        "roofline_gamma": gram_line,
         "kernels": per_kernel,
     }
     if not args.no_compare:

@@ -224,7 +224,7 @@ class Context:
     def set_tuning(self, amb_scale=-1.0, force_fp64=False):
         check(load().fpl_ctx_set_tuning(self.handle, float(amb_scale), int(force_fp64)), self.handle)
 
-    def set_shift(self, shift=0.99, backoff=0.97):
+    def set_shift(self, shift=0.999, backoff=0.97):
         """Shifts of the FP32 MLE inverse iteration (fpl_ctx_set_shift)."""
         check(load().fpl_ctx_set_shift(self.handle, float(shift), float(backoff)), self.handle)
 

@@ -17,7 +17,7 @@ constexpr size_t kCounterBlock = 64;
 // default tuning of the FP32 form
 constexpr float kDefaultAmbScale = 8.0f;    // FP32 rounding band, in units of n*eps*|A|_F
 constexpr float kDefaultCondMax = 1000.0f;  // |C| inverted in FP32 up to this inf-norm condition
-constexpr float kDefaultShift = 0.99f;      // inverse-iteration shift, in units of min(1, rho)
+constexpr float kDefaultShift = 0.999f;     // inverse-iteration shift, in units of min(1, rho)
 constexpr float kDefaultShiftBackoff = 0.97f;   // second shift when M - sigma I is not definite
 
 struct fpl_ctx {

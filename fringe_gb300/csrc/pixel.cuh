@@ -1710,7 +1710,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             C2<T> m0, m1;
             warp_matvec<T, LD, NP>(Wm, n, vv, m0, m1, lane);
             const T rho0 = warp_sum(ccmul(z0, m0).x + ccmul(z1, m1).x);
-            // P.shift (1%) below the Rayleigh quotient (or 1); if M - sigma I
+            // P.shift (0.1%) below the Rayleigh quotient (or 1); if M - sigma I
             // is not positive definite the shift was above lambda_1 and a
             // second attempt backs off to P.shift_backoff (3%) below
             const T rho1 = min(rho0, T(1));

@@ -233,7 +233,7 @@ const char *fpl_ctx_last_error(const fpl_ctx *ctx);
 int fpl_ctx_set_tuning(fpl_ctx *ctx, float amb_scale, int force_fp64);
 /* Shifts of the FP32 MLE inverse iteration, as fractions of min(1, rho) (rho
  * the Rayleigh quotient of the start vector): the first attempt and the
- * second one made when M - sigma I is not positive definite (defaults 0.99,
+ * second one made when M - sigma I is not positive definite (defaults 0.999,
  * 0.97).  A shift above 1 makes that attempt fail, which is how tests reach
  * the second attempt and the Householder path.  Runs and batches on this
  * context use them (servers and fpl_run_noalloc keep the defaults). */
