@@ -46,7 +46,7 @@
 namespace fpl {
 namespace {
 
-constexpr int BX_THREADS = 256;
+constexpr int BX_THREADS = 512;                    // 16 warps: the operand build hides latency
 constexpr int BX_TR = 8, BX_TC = 16, BX_M = 128;   // pixel tile (MMA M)
 constexpr int BX_NCOL = 256;                       // Gamma columns per pass (MMA N)
 constexpr int BX_MAXK = 2048;                      // union samples per tile
@@ -308,9 +308,11 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
     // (the first chunk's barriers order these before any use)
 
     // samples of chunk k0 (date pairs interleaved): each thread loads one
-    // sample for up to BX_XPT dates into registers; put() stores them in
-    // Xb and flags samples outside the split range for the stage's mask
-    constexpr int BX_XPT = 8;
+    // sample for up to BX_XPT dates into registers (32 dates at KC = 64,
+    // 64 at KC = 32, over the CTA); put() stores them in Xb and flags
+    // samples outside the split range for the stage's mask
+    constexpr int BX_XPT = (KC == 64 ? 32 : 64) * KC / BX_THREADS;
+    static_assert(BX_XPT >= 1 && BX_XPT * (BX_THREADS / KC) == (KC == 64 ? 32 : 64), "date coverage");
     const int sidx = tid % KC, d0 = tid / KC;
     float2 xv[BX_XPT];
     bool xbad = false;
@@ -381,15 +383,18 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
                     make_uint4(v[0], v[1], v[2], v[3]);
             }
             // ---- B: outer-product entries, hi and lo ----
-            for (int e = tid; e < 32 * (KC / 8); e += BX_THREADS) {
-                const int bl = e & 31, k8 = e >> 5;
+            // one thread per half core matrix: block bl's rows 4 ia .. 4 ia + 3
+            // (entries (2a + ia, 2b), (2a + ia, 2b + 1), Re and Im) over the 8
+            // samples of K group k8
+            for (int e = tid; e < 64 * (KC / 8); e += BX_THREADS) {
+                const int bl = e & 31, ia = (e >> 5) & 1, k8 = e >> 6;
                 if (bl * 8 >= nmma) continue;
-                unsigned char *dh = Bh + bl * L::SBO + k8 * 128;
-                unsigned char *dl = Bl + bl * L::SBO + k8 * 128;
+                unsigned char *dh = Bh + bl * L::SBO + k8 * 128 + ia * 64;
+                unsigned char *dl = Bl + bl * L::SBO + k8 * 128 + ia * 64;
                 if (bl * 8 >= ncol) {
                     const uint4 z = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) {
+                    for (int c = 0; c < 4; ++c) {
                         *reinterpret_cast<uint4 *>(dh + c * 16) = z;
                         *reinterpret_cast<uint4 *>(dl + c * 16) = z;
                     }
@@ -398,29 +403,24 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
                 const short2 ab = blk[cb / 8 + bl];
                 const unsigned char *xa = Xb + ab.x * L::XRS + k8 * 128;
                 const unsigned char *xb = Xb + ab.y * L::XRS + k8 * 128;
-                float4 pa[8], pb[8];   // per sample: x_{2a}, x_{2a+1} / x_{2b}, x_{2b+1}
+                float2 pa[8];          // per sample: x_{2a + ia}
+                float4 pb[8];          // per sample: x_{2b}, x_{2b+1}
 #pragma unroll
-                for (int q = 0; q < 8; ++q) pa[q] = *reinterpret_cast<const float4 *>(xa + q * 16);
-                if (ab.x != ab.y) {
+                for (int q = 0; q < 8; ++q) pa[q] = *reinterpret_cast<const float2 *>(xa + q * 16 + ia * 8);
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) pb[q] = *reinterpret_cast<const float4 *>(xb + q * 16);
-                } else {
+                for (int q = 0; q < 8; ++q) pb[q] = *reinterpret_cast<const float4 *>(xb + q * 16);
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) pb[q] = pa[q];
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int ia = u >> 1, jb = u & 1;     // i = 2a + ia, j = 2b + jb
+                for (int jb = 0; jb < 2; ++jb) {           // i = 2a + ia, j = 2b + jb
                     float re[8], im[8];
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
-                        const float xr = ia ? pa[q].z : pa[q].x, xi = ia ? pa[q].w : pa[q].y;
+                        const float xr = pa[q].x, xi = pa[q].y;
                         const float yr = jb ? pb[q].z : pb[q].x, yi = jb ? pb[q].w : pb[q].y;
                         re[q] = fmaf(xr, yr, xi * yi);          // Re x_i conj(x_j)
                         im[q] = fmaf(xi, yr, -(xr * yi));       // Im x_i conj(x_j)
                     }
-                    store_split(dh + (2 * u) * 16, dl + (2 * u) * 16, re);
-                    store_split(dh + (2 * u + 1) * 16, dl + (2 * u + 1) * 16, im);
+                    store_split(dh + (2 * jb) * 16, dl + (2 * jb) * 16, re);
+                    store_split(dh + (2 * jb + 1) * 16, dl + (2 * jb + 1) * 16, im);
                 }
             }
             fence_async_smem();
@@ -448,14 +448,15 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
         if (st.timed_out) return;
         if (!box_wait(mbar, st, 0) || !box_wait(mbar, st, 1)) { st.timed_out = true; break; }
         fence_after_sync();
-        // ---- epilogue: warp w reads TMEM lanes 32(w%4).., 128 columns ----
+        // ---- epilogue: warp w reads TMEM lanes 32(w%4).., BX_CPW x 32 columns ----
         {
+            constexpr int BX_CPW = (BX_NCOL / 32) / (BX_THREADS / 128);
             const int q = warp & 3, h = warp >> 2;
             const int m = 32 * q + lane;
             const bool store = pinfo[m] >= 0 && !pdefer[m];
             const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
             float *dst = reinterpret_cast<float *>(P.cbuf) + (store ? loc * P.cstride + cb : 0ll);
-            for (int c32 = 4 * h; c32 < 4 * h + 4; ++c32) {
+            for (int c32 = BX_CPW * h; c32 < BX_CPW * h + BX_CPW; ++c32) {
                 const int col0 = 32 * c32;
                 if (col0 >= ncol) break;
                 uint32_t v[32];
