@@ -416,33 +416,38 @@ def device_form(phase_link, d_stack, d_nmap, ctx, precision, method, steps, warm
 
 
 def nmap_measurement(stack, d_stack, ctx, steps, cpu_rows):
-    """The SHP map producer (fpl_nmap, KS2 test) on the same scene: device-
-    resident px/s over `steps` runs (each call ends with a stream sync), and
-    the oracle's restatement of the nmap module on the host cores over a row
-    sample."""
+    """The SHP map producer (fpl_nmap, KS2 and AD2 tests) on the same scene:
+    device-resident px/s over `steps` runs (each call ends with a stream
+    sync), and the oracle's restatement of the nmap module on the host cores
+    over a row sample."""
     import torch
     from fringe_gb300 import nmap
     nb, R, C = stack.shape
-    out = None
-    for _ in range(2):
-        out = nmap(d_stack, (NY, NX), ctx=ctx, out=out)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        nmap(d_stack, (NY, NX), ctx=ctx, out=out)
-    dt = (time.perf_counter() - t0) / steps
-    res = {"value": R * C / dt, "unit": "px/s", "ms_per_step": dt * 1e3,
-           "mean_count": float(out["count"].float().mean().item()),
-           "workload": "KS2 threshold 0.05 on the same %dx%d N=%d scene, half-window %dx%d" % (R, C, nb, NY, NX)}
-    if cpu_rows:
-        import oracle
-        rows = min(cpu_rows, R - 2 * NY)
+    res = {}
+    for method in ("KS2", "AD2"):
+        out = None
+        for _ in range(2):
+            out = nmap(d_stack, (NY, NX), ctx=ctx, out=out, method=method)
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        oracle.nmap(stack[:, :rows + 2 * NY], NY, NX, 0.05, nthreads=os.cpu_count() or 1)
-        dt = time.perf_counter() - t0
-        res["cpu_baseline"] = {"value": rows * C / dt, "unit": "px/s", "cores": os.cpu_count() or 1,
-                               "kind": "port", "sample": "%d rows (+%d apron rows) of the scene, %.1f s"
-                                                          % (rows, 2 * NY, dt)}
+        for _ in range(steps):
+            nmap(d_stack, (NY, NX), ctx=ctx, out=out, method=method)
+        dt = (time.perf_counter() - t0) / steps
+        r = {"value": R * C / dt, "unit": "px/s", "ms_per_step": dt * 1e3,
+             "mean_count": float(out["count"].float().mean().item()),
+             "workload": "%s threshold 0.05 on the same %dx%d N=%d scene, half-window %dx%d"
+                         % (method, R, C, nb, NY, NX)}
+        if cpu_rows:
+            import oracle
+            rows = min(cpu_rows, R - 2 * NY)
+            t0 = time.perf_counter()
+            oracle.nmap(stack[:, :rows + 2 * NY], NY, NX, 0.05, nthreads=os.cpu_count() or 1, method=method)
+            dt = time.perf_counter() - t0
+            r["cpu_baseline"] = {"value": rows * C / dt, "unit": "px/s", "cores": os.cpu_count() or 1,
+                                 "kind": "port", "sample": "%d rows (+%d apron rows) of the scene, %.1f s"
+                                                            % (rows, 2 * NY, dt)}
+        res[method.lower()] = r
+    res["value"] = res["ks2"]["value"]
     return res
 
 

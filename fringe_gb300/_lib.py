@@ -60,7 +60,10 @@ class FplNmapJob(ctypes.Structure):
                 ("half_window_y", ctypes.c_int), ("half_window_x", ctypes.c_int),
                 ("prob", ctypes.c_double), ("memory", ctypes.c_int),
                 ("stack", ctypes.c_void_p), ("mask", ctypes.c_void_p), ("amp_const", ctypes.c_void_p),
-                ("nmap", ctypes.c_void_p), ("count", ctypes.c_void_p)]
+                ("nmap", ctypes.c_void_p), ("count", ctypes.c_void_p), ("method", ctypes.c_int)]
+
+
+FPL_NMAP_METHOD = {"KS2": 0, "AD2": 1}
 
 
 class FplPsJob(ctypes.Structure):

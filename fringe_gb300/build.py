@@ -16,6 +16,7 @@ OBJDIR = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",      # host arithmetic as written (the AD2 threshold)
               "--expt-relaxed-constexpr"] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC"]
 

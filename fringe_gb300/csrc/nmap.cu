@@ -27,6 +27,20 @@
 //                series.  The test is symmetric, so testing every neighbour
 //                of every pixel gives the reference's half-window-and-mirror
 //                map exactly.
+//   k_nmap_tile<AD2> the same tile walk with the two-sample Anderson-Darling
+//                test (src/nmap/AD2unique.hpp:270-347).  The statistic is a
+//                sum over the merged walk, (2n m_j - n(j+1))^2 /
+//                ((j+1)(2n-j-1)) for the j+1 first values of which m_j come
+//                from the first sample, and the p-value decreases with it:
+//                the host finds the largest sum S* whose p-value, computed as
+//                the reference computes it, passes the threshold.  Each
+//                thread sums in FP32 and decides when it is clear of S* by
+//                a margin far above its rounding; otherwise it repeats the
+//                reference's own FP64 sum, operation for operation, and
+//                compares that with S*.  Ties are merged second sample
+//                first, so the test is not symmetric: every pair is tested
+//                with the reference's first sample, the pixel whose half-
+//                window loop (src/nmap/nmap.cpp:399-416) reaches the other.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -51,8 +65,12 @@ struct NmapParams {
     uint32_t *nmap;                  // [rows*cols][nulong]
     int32_t *count;                  // optional [rows*cols]
     double alpha[FPL_MAX_BANDS];     // normalised calibration constants
-    unsigned long long pass_lo;      // bit k (k < 64): D = k passes the threshold
-    unsigned pass_hi;                // bit 0: D = 64 passes
+    unsigned long long pass_lo;      // KS2: bit k (k < 64): D = k passes the threshold
+    unsigned pass_hi;                // KS2: bit 0: D = 64 passes
+    double ad_star;                  // AD2: largest walk sum whose p-value passes
+    float ad_lo, ad_hi;              // AD2: FP32 sums below ad_lo pass, above ad_hi fail
+    int ad_mode;                     // AD2: 0 compare, 1 every pair passes, 2 none does
+    float ad_w[2 * FPL_MAX_BANDS];   // AD2: n^2 / ((j+1)(2n-j-1)), j < 2n - 1
     long long plane;
     int rows, cols, nb, ny, nx, nulong, tr;
     int unit_alpha;                  // all constants 1: no division
@@ -135,7 +153,48 @@ __device__ __forceinline__ int ks_steps(const float *A, const float *B, int st, 
     return max(dm, abs(d));
 }
 
-__global__ void __launch_bounds__(256) k_nmap_ks(NmapParams P)
+// AD2: the walk sum of the first sample a over the merged order of two
+// ascending samples (a value of a goes first only when strictly smaller),
+// in FP32: the terms d^2 w_j, d = 2 m_j - (j + 1).
+__device__ __forceinline__ float ad_walk_fast(const float *A, const float *B, int st, int n, const float *w)
+{
+    int ia = 0, ib = 0;
+    float va = A[0], vb = B[0], s = 0.f;
+    for (int j = 0; j < 2 * n - 1; ++j) {
+        const bool ta = ia < n && (ib >= n || va < vb);
+        if (ta) {
+            ++ia;
+            if (ia < n) va = A[ia * st];
+        } else {
+            ++ib;
+            if (ib < n) vb = B[ib * st];
+        }
+        const int d = 2 * ia - (j + 1);
+        s = fmaf((float)(d * d), w[j], s);
+    }
+    return s;
+}
+
+// The same sum as the reference evaluates it (src/nmap/AD2unique.hpp:
+// 295-309), operation for operation in FP64: bit-identical to the host's.
+__device__ double ad_walk_exact(const float *A, const float *B, int st, int n)
+{
+    int ia = 0, ib = 0;
+    const double N = 2.0 * n, dn = n;
+    double m = 0.0, s = 0.0;
+    for (int j = 0; j < 2 * n - 1; ++j) {
+        const bool ta = ia < n && (ib >= n || A[ia * st] < B[ib * st]);
+        if (ta) ++ia; else ++ib;
+        m = __dadd_rn(m, ta ? 1.0 : 0.0);
+        const double bj = j + 1;
+        const double t = __dsub_rn(__dmul_rn(N, m), __dmul_rn(dn, bj));
+        s = __dadd_rn(s, __ddiv_rn(__dmul_rn(t, t), __dmul_rn(bj, __dsub_rn(N, bj))));
+    }
+    return s;
+}
+
+template <int AD2>
+__global__ void __launch_bounds__(256) k_nmap_tile(NmapParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int HW = NM_TC + 2 * P.nx, HH = P.tr + 2 * P.ny, HP = HW * HH;
@@ -144,6 +203,9 @@ __global__ void __launch_bounds__(256) k_nmap_ks(NmapParams P)
     const int SP = HP | 1;
     float *S = reinterpret_cast<float *>(smem);                       // [nb][SP]
     uint8_t *V = smem + sizeof(float) * (size_t)P.nb * SP;           // [HP]
+    __shared__ float W[2 * FPL_MAX_BANDS];
+    if (AD2)
+        for (int j = threadIdx.x; j < 2 * P.nb - 1; j += blockDim.x) W[j] = P.ad_w[j];
     const int ntc = (P.cols + NM_TC - 1) / NM_TC;
     const int R0 = (blockIdx.x / ntc) * P.tr, C0 = (blockIdx.x % ntc) * NM_TC;
     const int tid = threadIdx.x, nth = blockDim.x;
@@ -180,9 +242,20 @@ __global__ void __launch_bounds__(256) k_nmap_ks(NmapParams P)
             if (V[hq]) {
                 if (hq == hp) {
                     set = true;                                  // the centre (nmap.cpp:441-445)
-                } else {
+                } else if (!AD2) {
                     const int D = ks_steps(S + hp, S + hq, SP, P.nb);
                     set = (D < 64) ? ((P.pass_lo >> D) & 1ull) != 0 : (P.pass_hi & 1u) != 0;
+                } else if (P.ad_mode != 0) {
+                    set = P.ad_mode == 1;
+                } else {
+                    // the reference's first sample: this pixel when the
+                    // neighbour lies later in its half-window loop
+                    const bool fwd = ii > 0 || (ii == 0 && jj > 0);
+                    const float *A = S + (fwd ? hp : hq), *B = S + (fwd ? hq : hp);
+                    const float sf = ad_walk_fast(A, B, SP, P.nb, W);
+                    if (sf < P.ad_lo) set = true;
+                    else if (sf > P.ad_hi) set = false;
+                    else set = ad_walk_exact(A, B, SP, P.nb) <= P.ad_star;
                 }
             }
             if (set) {
@@ -224,6 +297,121 @@ double kolmogorov_prob(double z)
 // place of k/n; a table entry is accepted only when the decision is the
 // same over that whole interval (false: the threshold sits on the rounding
 // of a table value).
+// ---- AD2: the reference's p-value as a function of the walk sum ----------
+// Scholz & Stephens (1987), "K-sample Anderson-Darling tests", JASA 82:918:
+// the m = 1 column of their table of critical points of the standardised
+// statistic (the entries the reference reads, src/nmap/AD2unique.hpp:8-48
+// at indices 0, 8, .., 272), with the upper-tail probabilities it lists.
+const double kAdCrit[35] = {
+    -1.1954, -1.1786, -1.166, -1.1407, -1.1253, -1.0777, -1.0489, -0.9978, -0.9417, -0.8981, -0.8598, -0.7258,
+    -0.5966, -0.4572, -0.2966, -0.1009, 0.1571, 0.5357, 1.2255, 1.5262, 1.9633, 2.7314, 3.7825, 4.1241, 4.6044,
+    5.409, 6.4954, 6.8279, 7.2755, 8.1885, 9.3061, 9.6132, 10.0989, 10.8825, 11.8537};
+const double kAdProb[35] = {
+    .00001, .00005, .0001, .0005, .001, .005, .01, .025, .05, .075, .1, .2, .3, .4, .5, .6, .7, .8, .9,
+    .925, .95, .975, .99, .9925, .995, .9975, .999, .99925, .9995, .99975, .9999, .999925, .99995, .999975,
+    .99999};
+
+// sigma_N of the standardised statistic (Scholz & Stephens eq. 4, k = 2,
+// both samples of n; N = 2n < 2000, harmonic sums summed in the
+// reference's order, src/nmap/AD2unique.hpp:173-219)
+double ad_sigma(int n)
+{
+    const int N = 2 * n;
+    const double kk = 2.0, H = 1.0 / (1.0 * n) + 1.0 / (1.0 * n);
+    std::vector<double> inv(N > 1 ? N : 2, 0.0);
+    double h = 0.0, g = 0.0;
+    for (int i = 1; i < N; ++i) {
+        inv[i] = 1.0 / i;
+        h += inv[i];
+    }
+    for (int i = 1; i < N - 1; ++i) {
+        const double t = inv[N - i];
+        for (int j = i + 1; j < N; ++j) g += t * inv[j];
+    }
+    const double k2 = kk * kk;
+    const double a = (4 * g - 6) * (kk - 1) + (10 - 6 * g) * H;
+    const double b = (2 * g - 4) * k2 + 8 * h * kk + (2 * g - 14 * h - 4) * H - 8 * h + 4 * g - 6;
+    const double c = (6 * h + 2 * g - 2) * k2 + (4 * h - 4 * g + 6) * kk + (2 * h - 6) * H + 4 * h;
+    const double d = (2 * h + 6) * k2 - 4 * h * kk;
+    const double dN = (double)N;
+    double s2 = 0.0;
+    s2 += a * (dN * dN * dN) + b * (dN * dN) + c * N + d;
+    s2 /= ((double)(N - 1) * (double)(N - 2) * (double)(N - 3));
+    return std::sqrt(s2);
+}
+
+// the reference's p-value of the standardised statistic t (linear in
+// log((1 - p) / p) between the table's points, extrapolated past its ends)
+double ad_pvalue(double t)
+{
+    int i1 = -1;
+    for (int i = 0; i < 35; ++i) {
+        i1 = i - 1;
+        if (t <= kAdCrit[i]) break;
+    }
+    int i2 = i1 + 1;
+    if (i1 < 0) { i1 = 0; i2 = 1; }
+    if (i2 >= 35) { i1 = 33; i2 = 34; }
+    const double l1 = std::log((1.0 - kAdProb[i1]) / kAdProb[i1]), l2 = std::log((1.0 - kAdProb[i2]) / kAdProb[i2]);
+    const double t1 = kAdCrit[i1], t2 = kAdCrit[i2];
+    const double l0 = (l1 - l2) * (t - t2) / (t1 - t2) + l2;
+    return std::exp(l0) / (1. + std::exp(l0));
+}
+
+// does the walk sum s of a pair of n-date samples pass? (the chain of
+// src/nmap/AD2unique.hpp:333-345: both samples' sums are s)
+bool ad_pass(double s, int n, double sigma, double prob)
+{
+    double akn = 0.0;
+    akn = akn + s / (n * 1.0);
+    akn = akn + s / (n * 1.0);
+    akn = akn / (2.0 * n);
+    double t = akn - 1;
+    t /= sigma;
+    return ad_pvalue(t) >= prob;
+}
+
+// AD2 decision for this stack depth and threshold: the largest passing sum
+// S* (the pass set is every sum up to it); false when the decisions
+// within 4096 units in the last place of S* are not all on their side of it
+// (the threshold sits on the rounding of the p-value there).
+bool ad_table(int n, double prob, NmapParams *P)
+{
+    const double sigma = ad_sigma(n);
+    std::memset(P->ad_w, 0, sizeof(P->ad_w));
+    for (int j = 0; j < 2 * n - 1; ++j)
+        P->ad_w[j] = (float)((double)n * n / ((double)(j + 1) * (double)(2 * n - j - 1)));
+    const double top = 1e300;
+    const bool p0 = ad_pass(0.0, n, sigma, prob), p1 = ad_pass(top, n, sigma, prob);
+    P->ad_star = 0.0;
+    P->ad_lo = P->ad_hi = 0.f;
+    if (p0 == p1) {                       // one decision for every sum
+        P->ad_mode = p0 ? 1 : 2;
+        for (int k = 0; k < 64; ++k)
+            if (ad_pass(top * k / 64.0, n, sigma, prob) != p0) return false;
+        return true;
+    }
+    if (!p0) return false;                // the p-value must fall with the sum
+    auto bits = [](double x) { uint64_t u; std::memcpy(&u, &x, 8); return u; };
+    auto val = [](uint64_t u) { double x; std::memcpy(&x, &u, 8); return x; };
+    uint64_t lo = bits(0.0), hi = bits(top);
+    while (hi - lo > 1) {
+        const uint64_t mid = lo + (hi - lo) / 2;
+        if (ad_pass(val(mid), n, sigma, prob)) lo = mid; else hi = mid;
+    }
+    for (int64_t k = -4096; k <= 4096; ++k) {
+        const int64_t u = (int64_t)lo + k;
+        if (u < 0) continue;
+        if (ad_pass(val((uint64_t)u), n, sigma, prob) != (k <= 0)) return false;
+    }
+    const double star = val(lo);
+    P->ad_star = star;
+    P->ad_lo = (float)(star * (1.0 - 1e-4));
+    P->ad_hi = (float)(star * (1.0 + 1e-4));
+    P->ad_mode = 0;
+    return true;
+}
+
 bool ks_table(int n, double prob, unsigned long long *lo, unsigned *hi)
 {
     *lo = 0;
@@ -297,8 +485,14 @@ extern "C" int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job)
         P.alpha[b] = a[b];
         if (a[b] != 1.0) P.unit_alpha = 0;
     }
-    if (!ks_table(P.nb, job->prob, &P.pass_lo, &P.pass_hi)) {
+    if (job->method != FPL_NMAP_KS2 && job->method != FPL_NMAP_AD2) return FPL_ERR_OPTIONS;
+    const bool ad2 = job->method == FPL_NMAP_AD2;
+    if (!ad2 && !ks_table(P.nb, job->prob, &P.pass_lo, &P.pass_hi)) {
         ctx->last_error = "the threshold lies within rounding of a Kolmogorov table value for this stack depth";
+        return FPL_ERR_OPTIONS;
+    }
+    if (ad2 && !ad_table(P.nb, job->prob, &P)) {
+        ctx->last_error = "the threshold lies within rounding of the Anderson-Darling p-value for this stack depth";
         return FPL_ERR_OPTIONS;
     }
     size_t smem = 0;
@@ -356,11 +550,12 @@ extern "C" int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job)
     else if (P.nb <= 32) k_nmap_sort<32><<<sblocks, 128, 0, st>>>(P);
     else k_nmap_sort<64><<<sblocks, 128, 0, st>>>(P);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_sort");
-    if ((e = cudaFuncSetAttribute(k_nmap_ks, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024)) != cudaSuccess)
-        return fail(e, "k_nmap_ks attributes");
+    auto kern = ad2 ? k_nmap_tile<1> : k_nmap_tile<0>;
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+        return fail(e, "k_nmap_tile attributes");
     const long long ntiles = (long long)((P.cols + NM_TC - 1) / NM_TC) * ((P.rows + P.tr - 1) / P.tr);
-    k_nmap_ks<<<(unsigned)ntiles, NM_TC * P.tr, smem, st>>>(P);
-    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_ks");
+    kern<<<(unsigned)ntiles, NM_TC * P.tr, smem, st>>>(P);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_tile");
     if (job->memory == FPL_MEM_HOST) {
         if ((e = cudaMemcpyAsync(job->nmap, P.nmap, b_nmap, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
             return fail(e, "copy nmap");

@@ -153,11 +153,14 @@ class PhaseLinkBatch:
             pass
 
 
-def nmap(stack, half_window, prob=0.05, mask=None, amp_const=None, device=0, out=None, ctx=None):
-    """SHP neighbourhood map of a stack (the nmap module, KS2 method).
+def nmap(stack, half_window, prob=0.05, mask=None, amp_const=None, device=0, out=None, ctx=None,
+         method="KS2"):
+    """SHP neighbourhood map of a stack (the nmap module, KS2 or AD2 method).
 
     stack : complex64 [nbands, rows, cols], NumPy (host) or CUDA torch tensor.
     half_window : (Ny, Nx).  prob: similarity threshold (nmapOptions::prob).
+    method : "KS2" (two-sample Kolmogorov-Smirnov) or "AD2" (two-sample
+    Anderson-Darling), nmapOptions::method.
     mask : optional uint8 [rows, cols] (0 = excluded); amp_const: optional
     per-band amplitude calibration constants.  Returns dict(nmap uint32
     [rows, cols, nulong] (int32 for torch), count int32 [rows, cols]).
@@ -180,7 +183,7 @@ def nmap(stack, half_window, prob=0.05, mask=None, amp_const=None, device=0, out
         job = _lib.FplNmapJob(R, C, nb, ny, nx, float(prob), _lib.FPL_MEM_DEVICE, stack.data_ptr(),
                               m.data_ptr() if m is not None else None,
                               a.ctypes.data if a is not None else None,
-                              out["nmap"].data_ptr(), out["count"].data_ptr())
+                              out["nmap"].data_ptr(), out["count"].data_ptr(), _lib.FPL_NMAP_METHOD[method])
         _lib.check(lib.fpl_nmap(ctx.handle, ctypes.byref(job)), ctx.handle)
         return out
     stack = np.ascontiguousarray(stack, dtype=np.complex64)
@@ -191,7 +194,7 @@ def nmap(stack, half_window, prob=0.05, mask=None, amp_const=None, device=0, out
     job = _lib.FplNmapJob(R, C, nb, ny, nx, float(prob), _lib.FPL_MEM_HOST, stack.ctypes.data,
                           m.ctypes.data if m is not None else None,
                           a.ctypes.data if a is not None else None,
-                          out["nmap"].ctypes.data, out["count"].ctypes.data)
+                          out["nmap"].ctypes.data, out["count"].ctypes.data, _lib.FPL_NMAP_METHOD[method])
     _lib.check(lib.fpl_nmap(ctx.handle, ctypes.byref(job)), ctx.handle)
     return out
 

@@ -257,16 +257,23 @@ int fpl_ctx_profile_kernels(const fpl_ctx *ctx, double *ms, int count);
 
 /* ---- SHP neighbourhood map (the nmap module) --------------------------------
  * The producer of the nmap input: for every pixel, the two-sample
- * Kolmogorov-Smirnov test of its N amplitudes against those of each pixel of
+ * Kolmogorov-Smirnov (method FPL_NMAP_KS2) or Anderson-Darling
+ * (FPL_NMAP_AD2) test of its N amplitudes against those of each pixel of
  * its (2Ny+1) x (2Nx+1) window; the neighbour's bit is set (Ulongmask layout)
  * when the test's probability is >= prob, and the centre bit of every valid
- * pixel.  A pixel is valid when the optional mask is nonzero and all its
+ * pixel.  Each pair is tested with the reference's argument order (the pixel
+ * whose half-window loop reaches the other is the first sample), which
+ * matters for AD2 when the samples share values.  A pixel is valid when the optional mask is nonzero and all its
  * amplitudes |x_b| / alpha_b are nonzero and not NaN, alpha_b being the
  * band's "amplitudeConstant" normalised to the first band (<= 0 or absent:
  * 1).  Replaces the in-memory core of nmap_process (src/nmap/nmap.cpp:
- * 345-473; KS2 method, src/nmap/KS2sample.hpp:96-144).  Returns
- * FPL_ERR_OPTIONS when prob lies within rounding of one of the test's
- * discrete probability values for this stack depth (move it by 1e-12). */
+ * 345-473; nmapOptions::method "KS2" / "AD2", src/nmap/nmap.cpp:27-40,
+ * src/nmap/KS2sample.hpp:96-144, src/nmap/AD2unique.hpp:270-347).  Returns
+ * FPL_ERR_OPTIONS when prob lies within rounding of one of the KS test's
+ * discrete probability values for this stack depth, or of the AD test's
+ * p-value at its decision boundary (move it by 1e-12). */
+#define FPL_NMAP_KS2 0
+#define FPL_NMAP_AD2 1
 typedef struct {
     int rows, cols, nbands;
     int half_window_y, half_window_x;    /* nmapOptions::Ny, Nx (default 5, 5) */
@@ -277,6 +284,7 @@ typedef struct {
     const double *amp_const;             /* optional [nbands], host memory        */
     uint32_t *nmap;                      /* out [rows][cols][nulong]              */
     int32_t *count;                      /* optional out [rows][cols]: bits set   */
+    int method;                          /* FPL_NMAP_KS2 (default 0) or FPL_NMAP_AD2 */
 } fpl_nmap_job;
 
 int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job);

@@ -37,7 +37,10 @@ class _Params(ctypes.Structure):
 class _NmapParams(ctypes.Structure):
     _fields_ = [("rows", ctypes.c_int), ("cols", ctypes.c_int), ("nbands", ctypes.c_int),
                 ("ny", ctypes.c_int), ("nx", ctypes.c_int), ("prob", ctypes.c_double),
-                ("nthreads", ctypes.c_int)]
+                ("nthreads", ctypes.c_int), ("method", ctypes.c_int)]
+
+
+NMAP_METHODS = {"KS2": 0, "AD2": 1}
 
 
 def build_port(force=False):
@@ -95,6 +98,8 @@ def load(kind="port"):
     lib.fpl_oracle_nmap.restype = ctypes.c_int
     lib.fpl_oracle_ks2.argtypes = [ctypes.c_int, P, P]
     lib.fpl_oracle_ks2.restype = ctypes.c_double
+    lib.fpl_oracle_ad2.argtypes = [ctypes.c_int, P, P]
+    lib.fpl_oracle_ad2.restype = ctypes.c_double
     _LIBS[kind] = lib
     return lib
 
@@ -152,8 +157,8 @@ def pd_inverse(A, kind="port"):
     return info, a
 
 
-def nmap(stack, ny, nx, prob=0.05, mask=None, amp_const=None, nthreads=0, kind="port"):
-    """SHP map of the nmap module (KS2 method) over a whole scene.
+def nmap(stack, ny, nx, prob=0.05, mask=None, amp_const=None, nthreads=0, kind="port", method="KS2"):
+    """SHP map of the nmap module (method "KS2" or "AD2") over a whole scene.
 
     stack: complex64 [nbands, rows, cols]; mask: optional uint8 [rows, cols];
     amp_const: optional per-band calibration constants.  Returns
@@ -167,11 +172,22 @@ def nmap(stack, ny, nx, prob=0.05, mask=None, amp_const=None, nthreads=0, kind="
     count = np.zeros((R, C), np.int32)
     m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
     a = None if amp_const is None else np.ascontiguousarray(amp_const, dtype=np.float64)
-    p = _NmapParams(R, C, nb, ny, nx, float(prob), nthreads)
+    p = _NmapParams(R, C, nb, ny, nx, float(prob), nthreads, NMAP_METHODS[method])
     rc = lib.fpl_oracle_nmap(ctypes.byref(p), _ptr(stack), _ptr(m), _ptr(a), _ptr(out), _ptr(count))
     if rc != 0:
         raise ValueError("oracle rejected the parameters (%d)" % rc)
     return out, count
+
+
+def ad2(a, b, kind="port"):
+    """p-value of the two-sample Anderson-Darling test of two equal-length
+    samples (sorted ascending here, as the nmap module sorts them); a is the
+    reference's first argument."""
+    lib = load(kind)
+    a = np.ascontiguousarray(np.sort(np.asarray(a, np.float32)))
+    b = np.ascontiguousarray(np.sort(np.asarray(b, np.float32)))
+    assert a.shape == b.shape
+    return lib.fpl_oracle_ad2(len(a), _ptr(a), _ptr(b))
 
 
 def ks2(a, b, kind="port"):

@@ -76,7 +76,8 @@ int fpl_oracle_pd_inverse(int n, double *A);
 
 /* ---- SHP neighbourhood map (fpl_nmap_oracle.c) ---------------------------
  * The in-memory core of the nmap module (src/nmap/nmap.cpp:345-473) with
- * the two-sample Kolmogorov-Smirnov test.  stack as above; mask optional
+ * the two-sample Kolmogorov-Smirnov (KS2) or Anderson-Darling (AD2) test
+ * (nmapOptions::method, src/nmap/nmap.cpp:27-40).  stack as above; mask optional
  * [rows][cols] (0 = excluded); amp_const optional per-band amplitude
  * calibration constants (the "amplitudeConstant" item of each band, <= 0 or
  * NULL meaning 1); nmap [rows][cols][nulong] in the Ulongmask layout; count
@@ -86,13 +87,19 @@ typedef struct {
     int ny, nx;               /* half windows (lines, pixels) */
     double prob;              /* similarity threshold (nmapOptions::prob) */
     int nthreads;             /* <= 0: OpenMP default */
+    int method;               /* FPL_NMAP_KS2 or FPL_NMAP_AD2 */
 } fpl_nmap_params;
+
+#define FPL_NMAP_KS2 0
+#define FPL_NMAP_AD2 1
 
 int fpl_oracle_nmap(const fpl_nmap_params *p, const float *stack, const uint8_t *mask,
                     const double *amp_const, uint32_t *nmap, int32_t *count);
 
-/* The probability of one two-sample test of ascending arrays of length n. */
+/* The probability of one two-sample test of ascending arrays of length n
+ * (a is the reference's first argument, the centre pixel). */
 double fpl_oracle_ks2(int n, const float *a, const float *b);
+double fpl_oracle_ad2(int n, const float *a, const float *b);
 
 /* Which primitive provider this build uses: "port" or "reference". */
 const char *fpl_oracle_kind(void);

@@ -5,7 +5,8 @@
  * -DFPL_BACKEND_REF) call the reference's own, unmodified EVWorker
  * (include/fringe/EigenLapack.hpp:60-251), which in turn calls LAPACK
  * zheevr / zpotrf / zpotri, and the nmap oracle call the reference's own
- * two-sample KS test (src/nmap/KS2sample.hpp:96-144).  The headers are
+ * two-sample KS and Anderson-Darling tests (src/nmap/KS2sample.hpp:96-144,
+ * src/nmap/AD2unique.hpp:270-347).  The headers are
  * compiled where they lie in the reference tree (see build_ref.sh); nothing
  * from them is copied here.
  */
@@ -14,6 +15,7 @@
 
 #include "fringe/EigenLapack.hpp"
 #include "KS2sample.hpp"
+#include "AD2unique.hpp"
 
 extern "C" {
 
@@ -43,6 +45,20 @@ double fpl_ref_ks2(int n, const float *a, const float *b)
 {
     KS2sample ks(n);
     return ks.test(a, b);
+}
+
+// one test object per thread and stack depth (its constructor sums the
+// harmonic series of the variance, O(n^2))
+double fpl_ref_ad2(int n, const float *a, const float *b)
+{
+    static thread_local AD2unique *ad = nullptr;
+    static thread_local int ad_n = -1;
+    if (ad_n != n) {
+        delete ad;
+        ad = new AD2unique(n);
+        ad_n = n;
+    }
+    return ad->test(a, b);
 }
 
 }

@@ -36,15 +36,17 @@ def test_struct_layout_matches_header(lib, tmp_path):
     from fringe_gb300 import _lib
     src = tmp_path / "sz.c"
     src.write_text('#include "fringe_gb300.h"\n#include <stdio.h>\n#include <stddef.h>\n'
-                   'int main(){printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(fpl_job), sizeof(fpl_options),'
+                   'int main(){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(fpl_job), sizeof(fpl_options),'
                    ' sizeof(fpl_stats), offsetof(fpl_job, stack), offsetof(fpl_options, method),'
-                   ' sizeof(fpl_ps_job), offsetof(fpl_ps_job, tcorr_out));}\n')
+                   ' sizeof(fpl_ps_job), offsetof(fpl_ps_job, tcorr_out), sizeof(fpl_nmap_job),'
+                   ' offsetof(fpl_nmap_job, count), offsetof(fpl_nmap_job, method));}\n')
     exe = tmp_path / "sz"
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
     out = subprocess.check_output([str(exe)]).decode().split()
     want = [ctypes.sizeof(_lib.FplJob), ctypes.sizeof(_lib.FplOptions), ctypes.sizeof(_lib.FplStats),
             _lib.FplJob.stack.offset, _lib.FplOptions.method.offset,
-            ctypes.sizeof(_lib.FplPsJob), _lib.FplPsJob.tcorr_out.offset]
+            ctypes.sizeof(_lib.FplPsJob), _lib.FplPsJob.tcorr_out.offset, ctypes.sizeof(_lib.FplNmapJob),
+            _lib.FplNmapJob.count.offset, _lib.FplNmapJob.method.offset]
     assert [int(x) for x in out] == want
 
 

@@ -9,10 +9,10 @@ from fringe_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def _check(stack, ny, nx, prob=0.05, mask=None, amp_const=None):
+def _check(stack, ny, nx, prob=0.05, mask=None, amp_const=None, method="KS2"):
     from fringe_gb300 import nmap
-    g = nmap(stack, (ny, nx), prob=prob, mask=mask, amp_const=amp_const)
-    o_map, o_cnt = oracle.nmap(stack, ny, nx, prob, mask=mask, amp_const=amp_const)
+    g = nmap(stack, (ny, nx), prob=prob, mask=mask, amp_const=amp_const, method=method)
+    o_map, o_cnt = oracle.nmap(stack, ny, nx, prob, mask=mask, amp_const=amp_const, method=method)
     assert np.array_equal(g["count"], o_cnt), int((g["count"] != o_cnt).sum())
     assert np.array_equal(g["nmap"], o_map)
     return g
@@ -27,13 +27,15 @@ def _check(stack, ny, nx, prob=0.05, mask=None, amp_const=None):
     (12, 20, 64, 1, 2, 64),
     (10, 12, 1, 1, 1, 1),
 ])
-def test_nmap_matches_oracle(gpu_lib, R, C, N, ny, nx, seed):
+@pytest.mark.parametrize("method", ["KS2", "AD2"])
+def test_nmap_matches_oracle(gpu_lib, R, C, N, ny, nx, seed, method):
     stack, _ = synth.scene("voronoi", R, C, N, ny, nx, seed=seed)
-    g = _check(stack, ny, nx)
+    g = _check(stack, ny, nx, method=method)
     assert (g["count"] > 0).all()                     # every pixel valid: centre bit set
 
 
-def test_nmap_mask_constants_invalid_pixels_and_ties(gpu_lib):
+@pytest.mark.parametrize("method", ["KS2", "AD2"])
+def test_nmap_mask_constants_invalid_pixels_and_ties(gpu_lib, method):
     rng = np.random.default_rng(5)
     stack, _ = synth.scene("voronoi", 30, 40, 20, 3, 4, seed=8)
     stack[:, 5, 6] = 0                                # zero amplitude in every date
@@ -41,14 +43,34 @@ def test_nmap_mask_constants_invalid_pixels_and_ties(gpu_lib):
     stack[:, 20:24, 30:36] = np.round(stack[:, 20:24, 30:36].real * 2) / 2   # ties
     mask = (rng.random((30, 40)) > 0.05).astype(np.uint8)
     const = rng.uniform(0.5, 2.0, 20)
-    g = _check(stack, 3, 4, prob=0.1, mask=mask, amp_const=const)
+    g = _check(stack, 3, 4, prob=0.1, mask=mask, amp_const=const, method=method)
     assert g["count"][5, 6] == 0 and g["count"][9, 9] == 0
 
 
-def test_nmap_thresholds(gpu_lib):
+@pytest.mark.parametrize("method", ["KS2", "AD2"])
+def test_nmap_thresholds(gpu_lib, method):
     stack, _ = synth.scene("voronoi", 24, 30, 30, 2, 4, seed=11)
     for prob in (0.0, 0.01, 0.5, 0.9, 1.0):
-        _check(stack, 2, 4, prob=prob)
+        _check(stack, 2, 4, prob=prob, method=method)
+
+
+def test_ad2_ties_use_the_reference_argument_order(gpu_lib):
+    """Quantised amplitudes make neighbours share values, where the AD test
+    depends on which pixel is the first sample: the map still equals the
+    reference's (the golden maps its own tests wrote) bit for bit."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_nmap.npz"))
+    from fringe_gb300 import nmap
+    for name in ("voronoi", "ties"):
+        R, C, N, ny, nx = [int(x) for x in g[name + "/shape"]]
+        for m in ("KS2", "AD2"):
+            d = nmap(g[name + "/stack"], (ny, nx), method=m)
+            assert np.array_equal(d["nmap"], g["%s/%s_nmap" % (name, m)]), (name, m)
+            assert np.array_equal(d["count"], g["%s/%s_count" % (name, m)]), (name, m)
+    # a scene where every neighbour pair shares values
+    stack, _ = synth.scene("voronoi", 26, 34, 20, 3, 5, seed=31)
+    q = (np.round(np.abs(stack) * 2) / 2).astype(np.complex64)
+    _check(q, 3, 5, method="AD2")
 
 
 def test_nmap_device_path_feeds_phase_linking(gpu_lib):

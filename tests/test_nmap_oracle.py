@@ -1,6 +1,8 @@
 """CPU checks of the nmap oracle (test infrastructure): the port's two-sample
-KS test against the reference's own KS2sample (when the reference-linked
-oracle is built), known answers, and the structure of the map it builds."""
+KS and Anderson-Darling tests against the reference's own KS2sample and
+AD2unique (the reference-linked oracle where it is built; everywhere, the
+golden vectors it wrote, tests/golden/golden_nmap.npz), known answers, and
+the structure of the map it builds."""
 import os
 
 import numpy as np
@@ -34,13 +36,69 @@ def test_ks2_port_matches_reference_header():
             assert oracle.ks2(a, b, "port") == oracle.ks2(a, b, "reference")
 
 
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_nmap.npz")
+
+
+def test_port_matches_reference_golden_tests():
+    """Both tests, both argument orders, samples with and without shared
+    values: the port's probabilities equal the reference's bit for bit."""
+    g = np.load(GOLDEN)
+    for n in (2, 3, 5, 10, 16, 30, 45, 64):
+        a, b = g["pairs%d/a" % n], g["pairs%d/b" % n]
+        for m, f in (("ks2", oracle.ks2), ("ad2", oracle.ad2)):
+            ab = np.array([f(a[k], b[k]) for k in range(len(a))])
+            ba = np.array([f(b[k], a[k]) for k in range(len(a))])
+            assert np.array_equal(ab, g["pairs%d/%s_ab" % (n, m)]), (n, m)
+            assert np.array_equal(ba, g["pairs%d/%s_ba" % (n, m)]), (n, m)
+    # the AD test is not symmetric when the samples share values
+    assert not np.array_equal(g["pairs10/ad2_ab"], g["pairs10/ad2_ba"])
+    assert np.array_equal(g["pairs10/ks2_ab"], g["pairs10/ks2_ba"])
+
+
+def test_port_maps_match_reference_golden_maps():
+    g = np.load(GOLDEN)
+    for name in ("voronoi", "ties"):
+        R, C, N, ny, nx = [int(x) for x in g[name + "/shape"]]
+        for m in ("KS2", "AD2"):
+            mp, cnt = oracle.nmap(g[name + "/stack"], ny, nx, 0.05, method=m)
+            assert np.array_equal(mp, g["%s/%s_nmap" % (name, m)]), (name, m)
+            assert np.array_equal(cnt, g["%s/%s_count" % (name, m)]), (name, m)
+
+
+def test_ad2_known_answers():
+    """Identical samples give the smallest statistic (p near 1); disjoint
+    samples the largest (p near 0)."""
+    a = np.arange(1, 31, dtype=np.float32)
+    assert oracle.ad2(a, a) > 0.99
+    assert oracle.ad2(a, a + 100.0) < 1e-4
+    assert oracle.ad2(a + 100.0, a) < 1e-4
+
+
+@pytest.mark.skipif(not os.path.exists(oracle.REF_SO), reason="reference-linked oracle not built")
+def test_ad2_port_matches_reference_header():
+    """The port restates AD2unique::test (src/nmap/AD2unique.hpp:270-347);
+    the reference build runs the header itself."""
+    rng = np.random.default_rng(4)
+    for n in (1, 2, 5, 10, 30, 45, 64):
+        for _ in range(200):
+            a = rng.rayleigh(1.0, n).astype(np.float32)
+            b = (rng.rayleigh(1.0, n) * rng.uniform(0.5, 2.0)).astype(np.float32)
+            if rng.random() < 0.3:
+                a = np.round(a * 4) / 4
+                b = np.round(b * 4) / 4
+            pa, ra = oracle.ad2(a, b, "port"), oracle.ad2(a, b, "reference")
+            assert pa == ra or (np.isnan(pa) and np.isnan(ra))
+
+
 @pytest.mark.skipif(not os.path.exists(oracle.REF_SO), reason="reference-linked oracle not built")
 def test_nmap_port_matches_reference_build():
     stack, _ = synth.scene("voronoi", 24, 30, 12, 3, 5, seed=9)
     stack[:, 3, 4] = 0                                  # an invalid pixel
-    a = oracle.nmap(stack, 3, 5, 0.05, kind="port")
-    b = oracle.nmap(stack, 3, 5, 0.05, kind="reference")
-    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    stack[:, 10:14, 6:12] = np.round(stack[:, 10:14, 6:12].real)      # shared values
+    for m in ("KS2", "AD2"):
+        a = oracle.nmap(stack, 3, 5, 0.05, kind="port", method=m)
+        b = oracle.nmap(stack, 3, 5, 0.05, kind="reference", method=m)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), m
 
 
 def _bit(m, ny, nx, ii, jj):
