@@ -516,7 +516,7 @@ def batch_measurement(stack, nmap, seed=7):
     res = {"jobs": len(jobs), "pixels": px,
            "mix": "16 tiles 512^2..2048^2, N in {10,15,20,30,45}, half-window 5x10, EVD/MLE, miniStackCount 1..3"}
     for prec in ("mixed", "fp32"):
-        b = PhaseLinkBatch(jobs, graph=True, autotune=(prec == "fp32"), precision=prec)
+        b = PhaseLinkBatch(jobs, graph=True, autotune=True, precision=prec)
         for _ in range(2):
             b.run()
         torch.cuda.synchronize()

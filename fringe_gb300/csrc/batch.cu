@@ -554,6 +554,15 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
+        // one untimed run first: the candidates' times then exclude one-time
+        // costs (module loading, kernel attributes, first-touch of buffers)
+        if (batch_enqueue(b, b->cap_stream) != FPL_OK || cudaStreamSynchronize(b->cap_stream) != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaFree(d_sum);
+            fpl_batch_destroy(b);
+            return FPL_ERR_CUDA;
+        }
         for (BatchClass &k : b->classes) {
             // key: (NP, taps of the first job, mean SHP count of the class / 16)
             unsigned long long shp = 0, px = 0;

@@ -61,8 +61,9 @@ __device__ __forceinline__ void solve_pixel(const KParams &P, long long pp, unsi
 {
     if constexpr (NP <= 32) {
         const int npix = pixel_load_gamma<NP, false>(P, pp, sm, lane, A);
-        if (npix >= 0 && rows_coherence<NP>(P, pp, A, sm, cp, lane))
-            pixel_solve<float, NP>(P, pp, sm, lane, npix, cp);
+        float cfro = -1.f;
+        if (npix >= 0 && rows_coherence<NP>(P, pp, A, sm, cp, lane, &cfro))
+            pixel_solve<float, NP>(P, pp, sm, lane, npix, cp, cfro);
     } else if constexpr (std::is_same<CP, CRowsTmem<NP>>::value) {
         // two rows per lane: normalise in the slab, then copy the rows over
         const int npix = pixel_load_gamma<NP>(P, pp, sm, lane, A);

@@ -1213,6 +1213,10 @@ __device__ int warp_inverse_iteration(C2<T> *W, int n, T sigma, unsigned char *s
 // ------------------------------------------------------------------------
 // per-pixel driver
 // ------------------------------------------------------------------------
+// power iterations on C from the all-ones vector that start the MLE
+// inverse iteration
+constexpr int kPowerStartIters = 2;
+
 template <typename T> struct BlockShape;
 template <> struct BlockShape<float> { static constexpr int BR = 8; };
 template <> struct BlockShape<double> { static constexpr int BR = 4; };
@@ -1480,7 +1484,7 @@ __device__ int pixel_coherence(const KParams &P, long long pp, unsigned char *sm
 // phase_link.cpp:540-665.
 template <typename T, int NP, typename CP>
 __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, int lane, int npix,
-                            const CP &cp)
+                            const CP &cp, T cfro = T(-1))
 {
     using L = Lay<T, NP>;
     using RS = RowShape<NP>;
@@ -1573,7 +1577,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             put_code(P, pp, lane, -2);
             return;
         }
-        const T dC = fp32 ? amb * fro_c() : T(0);
+        const T dC = fp32 ? amb * (cfro >= T(0) ? cfro : fro_c()) : T(0);
         const int r = lam_min_test_c<T, LD, NP>(cp, Wm, col, n, thr, dC, lane);
         if (r == 0) { defer_fp64(P, pp, lane); return; }
         if (r < 0) { put_code(P, pp, lane, -2); return; }
@@ -1699,13 +1703,27 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         T tr = T(0);
         for (int i = lane; i < n; i += 32) tr += Wm[i * LD + i].x;
         tr = warp_sum(tr) / T(n);
-        dM = (fp32 && !plink) ? amb * fro(Wm) : T(0);
+        // rounding band of the decisions on M's eigenvalues, amb |M|_F.  The
+        // common path needs only sigma > 1e-6 + band, which the bound
+        // |M|_F <= sqrt(n) |inv|C||_inf (|M_ij| <= |inv|C|_ij|, and the
+        // 2-norm of the symmetric inv|C| is at most its inf-norm) settles
+        // without a pass over M; the exact value is formed while M is in Wm
+        // whenever a decision is not settled by the bound.
+        const bool need_band = fp32 && !plink;
+        dM = need_band ? amb * sqrt(T(n)) * xnorm : T(0);
+        bool dM_exact = !need_band;
+        auto exact_dM = [&]() {
+            if (!dM_exact) {
+                dM = amb * fro(Wm);
+                dM_exact = true;
+            }
+        };
         __syncwarp();
         bool done = false;
         if (fp32) {
             // inverse iteration from the EVD direction, shifted just below
             // the Rayleigh quotient (the smallest eigenvalue is close to 1)
-            warp_power_start<T, NP>(cp, n, 4, sm, lane, z0, z1);
+            warp_power_start<T, NP>(cp, n, kPowerStartIters, sm, lane, z0, z1);
             C2<T> *vv = reinterpret_cast<C2<T> *>(sm + L::vv);
             C2<T> m0, m1;
             warp_matvec<T, LD, NP>(Wm, n, vv, m0, m1, lane);
@@ -1716,6 +1734,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             const T rho1 = min(rho0, T(1));
             const T sigma = T(P.shift) * rho1;
             __syncwarp();
+            if (!(sigma > thr + dM)) exact_dM();               // M is still in Wm
             if (sigma > thr + dM) {
                 // one call site for the iteration and for rebuilding M (the
                 // factorisation consumes it), so each is inlined once
@@ -1742,6 +1761,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
                     } else {
                         sigma1 = T(P.shift_backoff) * rho1;
                     }
+                    if (!(sigma1 > thr + dM)) exact_dM();       // M was rebuilt in Wm
                     if (!(sigma1 > thr + dM)) {
                         st = -1;
                         break;
@@ -1756,6 +1776,7 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             eig_index = 1;
             eig_lo = T(-1e30);
             eig_hi = tr * T(1.0001);
+            exact_dM();            // M is in Wm (rebuilt after a failed attempt)
         }
     } else {
         bool ok = warp_power<T, NP>(cp, n, sm, lane, z0, z1, &lam);
@@ -1995,7 +2016,7 @@ __device__ void rows_from_smem(const CP &cp, const C2<T> *A, int lane)
 // when a result is not finite.
 template <int NP, typename CP>
 __device__ bool rows_coherence(const KParams &P, long long pp, const C2<float> *G, unsigned char *sm,
-                               const CP &cp, int lane)
+                               const CP &cp, int lane, float *cfro)
 {
     static_assert(NP <= 32 && NP % 8 == 0, "one row per lane");
     constexpr int LD = NP + 1;
@@ -2009,6 +2030,7 @@ __device__ bool rows_coherence(const KParams &P, long long pp, const C2<float> *
     }
     bad = __any_sync(0xffffffffu, bad);
     __syncwarp();
+    float fs = 0.f;                    // |C|_F^2, summed as the solver's own pass would
     if (!bad) {
         const float ri = (lane < n) ? yv[lane] : 0.f;
 #pragma unroll 1
@@ -2031,6 +2053,7 @@ __device__ bool rows_coherence(const KParams &P, long long pp, const C2<float> *
                         e = cmk<float>(1.f, 0.f);
                     }
                     bad |= !isfinite(e.x) || !isfinite(e.y);
+                    fs += cabs2(e);
                 }
                 v[k] = e;
             }
@@ -2039,6 +2062,7 @@ __device__ bool rows_coherence(const KParams &P, long long pp, const C2<float> *
         cp.fence();
         bad = __any_sync(0xffffffffu, bad);
     }
+    *cfro = sqrtf(warp_sum(fs));
     __syncwarp();
     if (bad) {
         // non-finite coherence: the first eigen call is reported as failed
