@@ -310,28 +310,30 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
     // samples of chunk k0 (date pairs interleaved): each thread loads one
     // sample for up to BX_XPT dates into registers (32 dates at KC = 64,
     // 64 at KC = 32, over the CTA); put() stores them in Xb and flags
-    // samples outside the split range for the stage's mask
+    // samples outside the split range for the stage's mask.  The loads run
+    // two chunks ahead of the build: chunk c waits in xa (c even) or xb
+    // (c odd), chosen by a branch so both stay in registers, and no copy
+    // between them waits for loads in flight.
     constexpr int BX_XPT = (KC == 64 ? 32 : 64) * KC / BX_THREADS;
     static_assert(BX_XPT >= 1 && BX_XPT * (BX_THREADS / KC) == (KC == 64 ? 32 : 64), "date coverage");
     const int sidx = tid % KC, d0 = tid / KC;
-    float2 xv[BX_XPT];
-    bool xbad = false;
-    auto fetch = [&](int k0) {
+    float2 xa[BX_XPT], xb[BX_XPT];
+    auto fetch = [&](int k0, float2 (&xo)[BX_XPT]) {
         const int k = k0 + sidx;
         const int ur = k / uwp, uc = k - ur * uwp;
         const int r = R0 - P.ny + ur, c = C0 - P.nx + uc;
         const bool valid = uc < uw && ur < uh && r >= 0 && r < rows && c >= 0 && c < cols;
         const float2 *src = P.stack + (valid ? (long long)r * cols + c : 0ll);
-        xbad = false;
 #pragma unroll
         for (int q = 0; q < BX_XPT; ++q) {
             const int d = d0 + q * (BX_THREADS / KC);
             float2 x = make_float2(0.f, 0.f);
             if (valid && d < n) x = __ldg(src + d * plane);
-            xv[q] = x;
+            xo[q] = x;
         }
     };
-    auto put = [&](uint32_t *bw) {
+    auto put = [&](uint32_t *bw, const float2 (&xv)[BX_XPT]) {
+        bool xbad = false;
 #pragma unroll
         for (int q = 0; q < BX_XPT; ++q) {
             const int d = d0 + q * (BX_THREADS / KC);
@@ -346,9 +348,12 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
         if (xbad) atomicOr(bw + (sidx >> 5), 1u << (sidx & 31));
     };
     // prologue: the first chunk of the tile into Xb (its stage's flags
-    // were cleared when that stage was last used, or at start-up)
-    fetch(0);
-    put(badw + (st.gstep & 1) * (KC / 32));
+    // were cleared when that stage was last used, or at start-up), the
+    // second one into xa
+    const int gtot = npass * nchunk;
+    fetch(0, xa);
+    put(badw + (st.gstep & 1) * (KC / 32), xa);
+    if (gtot > 1) fetch((1 % nchunk) * KC, xb);
     __syncthreads();
 
     for (int pass = 0; pass < npass && !st.timed_out; ++pass) {
@@ -363,10 +368,15 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
             unsigned char *Bh = As + L::A_BYTES, *Bl = Bh + L::B_BYTES;
             uint32_t *bw = badw + s * (KC / 32);
             const int k0 = ch * KC;
-            // the next chunk (the first chunk again after the last one of
-            // a pass) is loaded while this one is built
-            const bool more = (ch + 1 < nchunk) || (pass + 1 < npass);
-            if (more) fetch(ch + 1 < nchunk ? k0 + KC : 0);
+            // chunk g + 1 (the first chunk again after the last one of a
+            // pass) is in registers; chunk g + 2 is loaded while this one
+            // is built, into the array chunk g left
+            const int g = pass * nchunk + ch;
+            const bool more = g + 1 < gtot;
+            if (g + 2 < gtot) {
+                if (g & 1) fetch(((g + 2) % nchunk) * KC, xb);
+                else fetch(((g + 2) % nchunk) * KC, xa);
+            }
             if (tid < KC / 32) badw[(s ^ 1) * (KC / 32) + tid] = 0;   // for the next chunk
             // ---- A: SHP mask rows ----
             for (int e = tid; e < BX_M * (KC / 8); e += BX_THREADS) {
@@ -443,34 +453,52 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
             // every thread has finished building this chunk (barrier
             // above): the prefetched samples replace it in Xb; the next
             // iteration's wait is the barrier before they are read
-            if (more) put(badw + (s ^ 1) * (KC / 32));
+            if (more) {
+                if (g & 1) put(badw + (s ^ 1) * (KC / 32), xa);
+                else put(badw + (s ^ 1) * (KC / 32), xb);
+            }
         }
         if (st.timed_out) return;
         if (!box_wait(mbar, st, 0) || !box_wait(mbar, st, 1)) { st.timed_out = true; break; }
         fence_after_sync();
         // ---- epilogue: warp w reads TMEM lanes 32(w%4).., BX_CPW x 32 columns ----
+        // A lane holds its own pixel's columns; they are written out through
+        // a 32 x 32 staging tile per warp (in the operand stages, which no
+        // MMA reads any more: both stages were waited for above) so that
+        // each store instruction writes four pixels' 128 contiguous bytes
+        // instead of 32 pixels' 16.
         {
             constexpr int BX_CPW = (BX_NCOL / 32) / (BX_THREADS / 128);
+            constexpr int SROW = 36;                        // staging row stride (floats)
+            static_assert((BX_THREADS / 32) * 32 * SROW * 4 <= 2 * L::STAGE, "staging fits the stages");
+            float *stg = reinterpret_cast<float *>(smem) + warp * (32 * SROW);
+            float *rec = reinterpret_cast<float *>(P.cbuf);
             const int q = warp & 3, h = warp >> 2;
-            const int m = 32 * q + lane;
-            const bool store = pinfo[m] >= 0 && !pdefer[m];
-            const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
-            float *dst = reinterpret_cast<float *>(P.cbuf) + (store ? loc * P.cstride + cb : 0ll);
             for (int c32 = BX_CPW * h; c32 < BX_CPW * h + BX_CPW; ++c32) {
                 const int col0 = 32 * c32;
                 if (col0 >= ncol) break;
                 uint32_t v[32];
                 tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)col0, v);
                 tmem_wait_ld();
-                if (store) {
-                    const int lim = min(32, ncol - col0);
 #pragma unroll
-                    for (int j = 0; j < 32; j += 4)
-                        if (j < lim)
-                            *reinterpret_cast<float4 *>(dst + col0 + j) =
-                                make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
-                                            __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
+                for (int j = 0; j < 32; j += 4)
+                    *reinterpret_cast<float4 *>(stg + lane * SROW + j) =
+                        make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
+                                    __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
+                __syncwarp();
+                const int lim = min(32, ncol - col0);
+                const int j = 4 * (lane & 7);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int pl = 4 * i + (lane >> 3);          // pixel of the warp's 32
+                    const int m = 32 * q + pl;
+                    if (j < lim && pinfo[m] >= 0 && !pdefer[m]) {
+                        const long long loc = (long long)(R0 + m / BX_TC) * cols + (C0 + m % BX_TC) - P.cbase;
+                        *reinterpret_cast<float4 *>(rec + loc * P.cstride + cb + col0 + j) =
+                            *reinterpret_cast<const float4 *>(stg + pl * SROW + j);
+                    }
                 }
+                __syncwarp();
             }
         }
         fence_before_sync();
