@@ -146,7 +146,12 @@ cudaError_t launch_batch_np(const BatchEntry *jobs, int njobs, long long total, 
 template <int NP>
 cudaError_t launch_batch64_np(const BatchEntry *jobs, int njobs, int num_sms, cudaStream_t st)
 {
-    const int warps = max_warps(NP, true);
+    // warps per CTA: shared memory's limit, and no more threads than the
+    // kernel's registers allow in one CTA
+    cudaFuncAttributes fa;
+    cudaError_t ea = cudaFuncGetAttributes(&fa, k_batch_fp64<NP>);
+    if (ea != cudaSuccess) return ea;
+    const int warps = std::max(1, std::min(max_warps(NP, true), fa.maxThreadsPerBlock / 32));
     const size_t smem = Lay<double, NP>::bytes * warps;
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fp64<NP>, warps * 32, smem);

@@ -261,6 +261,20 @@ static cudaError_t launch_t(const KParams &P, int num_sms, cudaStream_t st)
     int warps = int(budget / per_warp);
     if (warps > 16) warps = 16;
     if (CInTmem<T, NP>::value && warps > 4) warps = 4;   // one tensor-memory lane quadrant per warp
+    // and no more threads than the kernel's registers allow in one CTA
+    static int max_threads[64] = {0};
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev < 64 && !max_threads[dev]) {
+            cudaFuncAttributes fa;
+            cudaError_t e = cudaFuncGetAttributes(&fa, k_pixels<T, NP>);
+            if (e != cudaSuccess) return e;
+            max_threads[dev] = fa.maxThreadsPerBlock;
+        }
+        const int lim = (dev < 64 ? max_threads[dev] : 1024) / 32;
+        if (warps > lim) warps = lim;
+    }
     if (warps < 1) warps = 1;
     const size_t smem = per_warp * warps;
     int dev = 0;
