@@ -166,7 +166,7 @@ int fpl_ctx_destroy(fpl_ctx *ctx)
     if (ctx->s_out) cudaStreamDestroy(ctx->s_out);
     void *bufs[] = {ctx->d_stack, ctx->d_nmap, ctx->d_phase, ctx->d_tcorr, ctx->d_comp,
                     ctx->d_status, ctx->d_fb_list, ctx->d_small, ctx->d_cbuf, ctx->d_cinfo,
-                    ctx->d_nm};
+                    ctx->d_nm, ctx->d_pack};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (ctx->ev_last) cudaEventDestroy(ctx->ev_last);
@@ -188,13 +188,13 @@ int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out)
 
 static int fpl_enqueue_body(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
                             void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
-                            bool fp64_all, void *counters, bool count_run);
+                            bool fp64_all, void *counters, bool count_run, int stages, long long list_cap);
 
 // Enqueues both passes on `st` for device buffers.  Scratch: the context's
 // work-list buffer (grown with cudaMalloc when too small) and d_small.
 int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
                 void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
-                bool fp64_all, void *counters, bool count_run)
+                bool fp64_all, void *counters, bool count_run, int stages, long long list_cap)
 {
     if (!counters) counters = ctx->d_small;
     // runs sharing this context share its scratch: a run waits for the
@@ -204,7 +204,8 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
     FPL_CUDA(ctx, cudaStreamIsCapturing(st, &cap));
     const bool order = (cap == cudaStreamCaptureStatusNone);
     if (order && ctx->last_used) FPL_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_last, 0));
-    int rc_ = fpl_enqueue_body(ctx, job, stack, nmap, phase, tcorr, comp, status, st, fp64_all, counters, count_run);
+    int rc_ = fpl_enqueue_body(ctx, job, stack, nmap, phase, tcorr, comp, status, st, fp64_all, counters,
+                               count_run, stages, list_cap);
     if (rc_) return rc_;
     if (order) {
         FPL_CUDA(ctx, cudaEventRecord(ctx->ev_last, st));
@@ -215,7 +216,7 @@ int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint3
 
 static int fpl_enqueue_body(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
                             void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
-                            bool fp64_all, void *counters, bool count_run)
+                            bool fp64_all, void *counters, bool count_run, int stages, long long list_cap)
 {
     const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
     int rc = 0;
@@ -252,18 +253,21 @@ static int fpl_enqueue_body(fpl_ctx *ctx, const fpl_job *job, const void *stack,
     P.fb_count = d_count;
     P.err = d_err;
     P.slow = reinterpret_cast<int *>(static_cast<char *>(counters) + 32);
-    // work list: at most one entry per pixel of the range
-    size_t need = sizeof(long long) * (size_t)(P.npix > 0 ? P.npix : 1);
+    // work list: at most one entry per pixel of the range (or of the run)
+    const long long cap = list_cap > 0 ? list_cap : P.npix;
+    size_t need = sizeof(long long) * (size_t)(cap > 0 ? cap : 1);
     rc = grow(ctx, &ctx->d_fb_list, &ctx->cap_fb_list, need);
     if (rc) return rc;
     P.fb_list = static_cast<long long *>(ctx->d_fb_list);
-    P.fb_cap = (int)(P.npix < 0x7fffffff ? P.npix : 0x7fffffff);
-    FPL_CUDA(ctx, cudaMemsetAsync(counters, 0, kCounterBlock, st));
+    P.fb_cap = (int)(cap < 0x7fffffff ? cap : 0x7fffffff);
+    if (stages & ENQ_RESET) FPL_CUDA(ctx, cudaMemsetAsync(counters, 0, kCounterBlock, st));
     if (P.npix == 0) return FPL_OK;
     if (fp64_all) {
-        KParams Q = P;
-        Q.fb_list = nullptr;
-        FPL_CUDA(ctx, fpl::launch_fp64(Q, ctx->num_sms, st));
+        if (stages & ENQ_KERNELS) {
+            KParams Q = P;
+            Q.fb_list = nullptr;
+            FPL_CUDA(ctx, fpl::launch_fp64(Q, ctx->num_sms, st));
+        }
         return FPL_OK;
     }
     // optional per-kernel event pairs (fpl_ctx_set_profiling)
@@ -285,7 +289,9 @@ static int fpl_enqueue_body(fpl_ctx *ctx, const fpl_job *job, const void *stack,
     };
     if (ctx->profile && count_run) ctx->prof_runs++;
     const bool mixed = job->precision == FPL_PREC_MIXED && fpl::gram_box_supported(P.nb, P.ny, P.nx);
-    if (mixed) {
+    if (!(stages & ENQ_KERNELS)) {
+        // settle only
+    } else if (mixed) {
         // tensor-core Gamma records, then eigen-solves, chunk by chunk of
         // rows so the records stay within a bounded buffer
         const int rec = fpl::gram_box_record(P.nb);
@@ -309,8 +315,32 @@ static int fpl_enqueue_body(fpl_ctx *ctx, const fpl_job *job, const void *stack,
     } else {
         FPL_CUDA(ctx, timed(FPL_KTAG_FP32, [&] { return fpl::launch_fp32(P, ctx->num_sms, st); }));
     }
-    FPL_CUDA(ctx, timed(FPL_KTAG_FP64, [&] { return fpl::launch_fp64(P, ctx->num_sms, st); }));
+    if (stages & ENQ_SETTLE)
+        FPL_CUDA(ctx, timed(FPL_KTAG_FP64, [&] { return fpl::launch_fp64(P, ctx->num_sms, st); }));
     return FPL_OK;
+}
+
+// Outputs of the pixels on a run's FP64 work list, packed (nb + 3 complex
+// slots per pixel: the phases, the compressed SLC, {tcorr, status bits},
+// {pixel index low, high bits}) for one copy back to the host.
+__global__ void k_pack_settled(const long long *__restrict__ list, const int *__restrict__ count, int cap,
+                               const float2 *__restrict__ phase, const float *__restrict__ tcorr,
+                               const float2 *__restrict__ comp, const int32_t *__restrict__ status,
+                               long long plane, int nb, float2 *__restrict__ out)
+{
+    const int n = min(*count, cap);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < (long long)n * (nb + 3);
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long e = k / (nb + 3);
+        const int slot = (int)(k - e * (nb + 3));
+        const long long pp = list[e];
+        float2 v;
+        if (slot < nb) v = phase[slot * plane + pp];
+        else if (slot == nb) v = comp[pp];
+        else if (slot == nb + 1) v = make_float2(tcorr[pp], __int_as_float(status ? status[pp] : 0));
+        else v = make_float2(__int_as_float((int)(pp & 0xffffffffll)), __int_as_float((int)(pp >> 32)));
+        out[k] = v;
+    }
 }
 
 extern "C" {
@@ -415,7 +445,13 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job)
             if (span <= 0) cb[1] = r1;
         }
         int copied = std::max(0, r0 / 8 * 8 - ny);     // first stack row on the device
+        // One work list for the whole run: the chunks append to it and its
+        // FP64 settle runs once, after the last chunk (a settle per chunk
+        // costs a round of the slow FP64 pixels each time); the settled
+        // pixels' outputs then come back packed and are put in place here.
+        const long long run_px = (long long)(r1 - r0) * cols;
         FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+        bool first = true;                  // the first chunk clears the counters (starts the list)
         for (int c = 0; c < nchunks; ++c) {
             const int a = cb[c], b = cb[c + 1];
             if (b <= a) continue;
@@ -437,8 +473,9 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job)
             cj.row_begin = a;
             cj.row_end = b;
             rc = fpl_enqueue(ctx, &cj, d_stack, d_nmap, d_phase, d_tcorr, d_comp, d_status, st, ctx->force_fp64,
-                             static_cast<char *>(ctx->d_small) + kCounterBlock * c, c == 0);
+                             ctx->d_small, first, ENQ_KERNELS | (first ? ENQ_RESET : 0), run_px);
             if (rc) return rc;
+            first = false;
             FPL_CUDA(ctx, cudaEventRecord(ev_done, st));
             FPL_CUDA(ctx, cudaStreamWaitEvent(ctx->s_out, ev_done, 0));
             const size_t off = (size_t)a * cols, cnt = (size_t)(b - a) * cols;
@@ -452,23 +489,58 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job)
                 FPL_CUDA(ctx, cudaMemcpyAsync(job->status + off, d_status + off, cnt * 4, cudaMemcpyDeviceToHost,
                                               ctx->s_out));
         }
+        // the FP64 settle of every chunk's list, on the whole range (an empty
+        // range only clears the counters)
+        rc = fpl_enqueue(ctx, job, d_stack, d_nmap, d_phase, d_tcorr, d_comp, d_status, st, ctx->force_fp64,
+                         ctx->d_small, false, first ? ENQ_RESET : ENQ_SETTLE, run_px);
+        if (rc) return rc;
         FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
-        // the outputs and the counters are read once every chunk is done
-        FPL_CUDA(ctx, cudaStreamWaitEvent(st, ctx->chunk_ev[2 * (nchunks - 1) + 1], 0));
+        int head[16];
+        FPL_CUDA(ctx, cudaMemcpyAsync(head, ctx->d_small, kCounterBlock, cudaMemcpyDeviceToHost, st));
+        FPL_CUDA(ctx, cudaStreamSynchronize(st));
+        const long long nset = std::min<long long>(head[0], run_px);
+        if (nset > 0 && !ctx->force_fp64) {
+            const size_t slots = (size_t)nset * (nb + 3);
+            if ((rc = grow(ctx, &ctx->d_pack, &ctx->cap_pack, slots * sizeof(float2)))) return rc;
+            const unsigned blocks = (unsigned)std::min<size_t>((slots + 255) / 256, (size_t)ctx->num_sms * 8);
+            k_pack_settled<<<blocks, 256, 0, st>>>(static_cast<const long long *>(ctx->d_fb_list),
+                                                   static_cast<const int *>(ctx->d_small), (int)nset,
+                                                   reinterpret_cast<const float2 *>(d_phase), d_tcorr,
+                                                   reinterpret_cast<const float2 *>(d_comp), d_status, (long long)plane,
+                                                   nb, static_cast<float2 *>(ctx->d_pack));
+            FPL_CUDA(ctx, cudaGetLastError());
+            ctx->h_pack.resize(slots);
+            FPL_CUDA(ctx, cudaMemcpyAsync(ctx->h_pack.data(), ctx->d_pack, slots * sizeof(float2),
+                                          cudaMemcpyDeviceToHost, st));
+            FPL_CUDA(ctx, cudaStreamSynchronize(st));
+        }
+        // every chunk's outputs are on the host before the settled pixels
+        // are put in place over them
         FPL_CUDA(ctx, cudaStreamSynchronize(ctx->s_out));
+        if (nset > 0 && !ctx->force_fp64) {
+            float2 *h_phase = static_cast<float2 *>(job->phase), *h_comp = static_cast<float2 *>(job->comp);
+            for (long long e = 0; e < nset; ++e) {
+                const float2 *v = ctx->h_pack.data() + (size_t)e * (nb + 3);
+                uint32_t lo, hi;
+                int32_t stv;
+                std::memcpy(&lo, &v[nb + 2].x, 4);
+                std::memcpy(&hi, &v[nb + 2].y, 4);
+                std::memcpy(&stv, &v[nb + 1].y, 4);
+                const long long pp = (long long)(((uint64_t)hi << 32) | lo);
+                for (int b = 0; b < nb; ++b) h_phase[(size_t)b * plane + pp] = v[b];
+                h_comp[pp] = v[nb];
+                job->tcorr[pp] = v[nb + 1].x;
+                if (job->status) job->status[pp] = stv;
+            }
+        }
     }
-    int small[16 * kRunChunks];
-    FPL_CUDA(ctx, cudaMemcpyAsync(small, ctx->d_small, kCounterBlock * nchunks, cudaMemcpyDeviceToHost, st));
+    int small[16];
+    FPL_CUDA(ctx, cudaMemcpyAsync(small, ctx->d_small, kCounterBlock, cudaMemcpyDeviceToHost, st));
     FPL_CUDA(ctx, cudaStreamSynchronize(st));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    long long fp64 = 0, slow = 0;
-    unsigned err = 0;
-    for (int c = 0; c < nchunks; ++c) {
-        fp64 += small[16 * c];
-        err |= static_cast<unsigned>(small[16 * c + 4]);
-        slow += small[16 * c + 8];
-    }
+    const long long fp64 = small[0], slow = small[8];
+    const unsigned err = static_cast<unsigned>(small[4]);
     ctx->stats.pixels = (long long)(r1 - r0) * cols;
     ctx->stats.fp64_pixels = ctx->force_fp64 ? ctx->stats.pixels : fp64;
     ctx->stats.mixed_fp64_inverse = 0;

@@ -44,6 +44,11 @@ struct fpl_ctx {
     // nmap: sorted amplitudes, validity and staging of host jobs
     void *d_nm = nullptr;
     size_t cap_nm = 0;
+    // host-memory runs: outputs of the FP64-settled pixels, packed for the
+    // copy back (device) and received (host)
+    void *d_pack = nullptr;
+    size_t cap_pack = 0;
+    std::vector<float2> h_pack;
     // tuning
     float amb_scale = kDefaultAmbScale;
     float cond_max = kDefaultCondMax;
@@ -63,9 +68,17 @@ struct fpl_ctx {
 };
 
 int fpl_validate_job(const fpl_job *job);
+// What one fpl_enqueue call enqueues: the FP32 / mixed kernels, the FP64
+// settle of the pixels on the work list, and the clearing of the counters
+// (which starts a new work list).
+enum { ENQ_KERNELS = 1, ENQ_SETTLE = 2, ENQ_RESET = 4, ENQ_ALL = 7 };
 // Enqueues one run (rows [row_begin, row_end) of job) on st for device
 // buffers; counters: a kCounterBlock-byte block of device memory (NULL: the
-// context's first block); count_run: count it as a run for the profiler.
+// context's first block); count_run: count it as a run for the profiler;
+// list_cap: entries of the work list (0: the pixels of the row range; a
+// run enqueued as several row ranges with one settle at the end passes the
+// pixels of the whole run).
 int fpl_enqueue(fpl_ctx *ctx, const fpl_job *job, const void *stack, const uint32_t *nmap,
                 void *phase, float *tcorr, void *comp, int32_t *status, cudaStream_t st,
-                bool fp64_all, void *counters = nullptr, bool count_run = true);
+                bool fp64_all, void *counters = nullptr, bool count_run = true, int stages = ENQ_ALL,
+                long long list_cap = 0);
