@@ -282,7 +282,7 @@ def serving_measurement(njobs, seed=5):
         picks = rng.integers(0, len(pool), njobs)
         outs = [outputs(p) for p in picks]
         methods = rng.choice(["MLE", "EVD"], njobs)
-        srv = Server(memory_budget=80 << 30, wave_pixels=1 << 19)
+        srv = Server(memory_budget=80 << 30, wave_pixels=1 << 20)
         # warm-up (kernel loading, allocator)
         st, nm, hw = pool[0]
         srv.wait(srv.submit(st, nm, hw, precision=prec))

@@ -58,9 +58,15 @@ constexpr unsigned ERR_TC_TIMEOUT = 2u;
 constexpr long long BX_SPIN_LIMIT = 1ll << 26;     // ~ seconds of polling
 
 template <int KC> struct BoxLay {
+    // tensor-memory accumulators of BX_NCOL columns each: with 32-sample
+    // chunks two fit beside two operand stages, so a pass covers 512 Gamma
+    // columns and a chunk's samples and mask are loaded and built once for
+    // both
+    static constexpr int NACC = (KC == 32) ? 2 : 1;
+    static constexpr int PCOL = NACC * BX_NCOL;               // Gamma columns per pass
     static constexpr int SBO = KC * 16 + 16;                 // bytes between 8-row groups
     static constexpr int A_BYTES = (BX_M / 8) * SBO;
-    static constexpr int B_BYTES = (BX_NCOL / 8) * SBO;      // one of hi / lo
+    static constexpr int B_BYTES = (PCOL / 8) * SBO;         // one of hi / lo
     static constexpr int STAGE = A_BYTES + 2 * B_BYTES;
     static constexpr int MAXPAIR = (KC == 64) ? 16 : 32;     // date pairs: 32 or 64 dates
     static constexpr int XRS = KC * 16 + 16;                 // bytes per date-pair row of X
@@ -244,7 +250,7 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
     const int W = kp >> 5;
     const int ra = int(P.pix_begin / cols), rb = ra + int(P.npix / cols);
     const int ntc = (cols + BX_TC - 1) / BX_TC;
-    const int npass = (ncolt + BX_NCOL - 1) / BX_NCOL;
+    const int npass = (ncolt + L::PCOL - 1) / L::PCOL;
     const int min_neigh = (P.semantics == SEM_PL) ? P.min_neigh : 2;   // evd.cpp:566
     const long long plane = P.plane;
     const int R0 = box_first_row(P) + int(t / ntc) * BX_TR, C0 = int(t % ntc) * BX_TC;
@@ -357,10 +363,17 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
     __syncthreads();
 
     for (int pass = 0; pass < npass && !st.timed_out; ++pass) {
-        const int cb = pass * BX_NCOL;
-        const int ncol = min(BX_NCOL, ncolt - cb);
-        const int nmma = (ncol + 15) & ~15;
-        const uint32_t idesc = make_idesc(nmma);
+        const int cb = pass * L::PCOL;
+        const int ncol = min(L::PCOL, ncolt - cb);
+        // accumulator j holds the pass's columns [256 j, 256 j + 256)
+        int nmma[L::NACC];
+        uint32_t idesc[L::NACC];
+#pragma unroll
+        for (int j = 0; j < L::NACC; ++j) {
+            const int nc = min(BX_NCOL, ncol - j * BX_NCOL);
+            nmma[j] = nc > 0 ? (nc + 15) & ~15 : 0;
+            idesc[j] = make_idesc(nmma[j] > 0 ? nmma[j] : 16);
+        }
         for (int ch = 0; ch < nchunk; ++ch) {
             const int s = st.gstep & 1;
             if (!box_wait(mbar, st, s)) { st.timed_out = true; break; }
@@ -396,9 +409,12 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
             // one thread per half core matrix: block bl's rows 4 ia .. 4 ia + 3
             // (entries (2a + ia, 2b), (2a + ia, 2b + 1), Re and Im) over the 8
             // samples of K group k8
-            for (int e = tid; e < 64 * (KC / 8); e += BX_THREADS) {
-                const int bl = e & 31, ia = (e >> 5) & 1, k8 = e >> 6;
-                if (bl * 8 >= nmma) continue;
+            constexpr int NBL = L::PCOL / 8;                 // column blocks of the pass
+            for (int e = tid; e < 2 * NBL * (KC / 8); e += BX_THREADS) {
+                const int bl = e % NBL, ia = (e / NBL) & 1, k8 = e / (2 * NBL);
+                const int jacc = bl / (BX_NCOL / 8);
+                const int nm_j = (jacc == 0) ? nmma[0] : nmma[L::NACC - 1];
+                if ((bl - jacc * (BX_NCOL / 8)) * 8 >= nm_j) continue;          // read by no MMA
                 unsigned char *dh = Bh + bl * L::SBO + k8 * 128 + ia * 64;
                 unsigned char *dl = Bl + bl * L::SBO + k8 * 128 + ia * 64;
                 if (bl * 8 >= ncol) {
@@ -411,14 +427,14 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
                     continue;
                 }
                 const short2 ab = blk[cb / 8 + bl];
-                const unsigned char *xa = Xb + ab.x * L::XRS + k8 * 128;
-                const unsigned char *xb = Xb + ab.y * L::XRS + k8 * 128;
+                const unsigned char *sa = Xb + ab.x * L::XRS + k8 * 128;
+                const unsigned char *sb = Xb + ab.y * L::XRS + k8 * 128;
                 float2 pa[8];          // per sample: x_{2a + ia}
                 float4 pb[8];          // per sample: x_{2b}, x_{2b+1}
 #pragma unroll
-                for (int q = 0; q < 8; ++q) pa[q] = *reinterpret_cast<const float2 *>(xa + q * 16 + ia * 8);
+                for (int q = 0; q < 8; ++q) pa[q] = *reinterpret_cast<const float2 *>(sa + q * 16 + ia * 8);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) pb[q] = *reinterpret_cast<const float4 *>(xb + q * 16);
+                for (int q = 0; q < 8; ++q) pb[q] = *reinterpret_cast<const float4 *>(sb + q * 16);
 #pragma unroll
                 for (int jb = 0; jb < 2; ++jb) {           // i = 2a + ia, j = 2b + jb
                     float re[8], im[8];
@@ -441,10 +457,16 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
 #pragma unroll
                 for (int kk = 0; kk < KC / 16; ++kk) {
                     const uint64_t da = make_smem_desc(a0 + kk * 256, 128, L::SBO);
-                    const uint64_t dh = make_smem_desc(h0 + kk * 256, 128, L::SBO);
-                    const uint64_t dl = make_smem_desc(l0 + kk * 256, 128, L::SBO);
-                    tc_mma(tbase, da, dh, idesc, (ch > 0 || kk > 0) ? 1u : 0u);
-                    tc_mma(tbase, da, dl, idesc, 1u);
+#pragma unroll
+                    for (int j = 0; j < L::NACC; ++j) {
+                        if (nmma[j] == 0) continue;
+                        const uint32_t boff = (uint32_t)(j * (BX_NCOL / 8) * L::SBO + kk * 256);
+                        const uint64_t dh = make_smem_desc(h0 + boff, 128, L::SBO);
+                        const uint64_t dl = make_smem_desc(l0 + boff, 128, L::SBO);
+                        const uint32_t dt = tbase + (uint32_t)(j * BX_NCOL);
+                        tc_mma(dt, da, dh, idesc[j], (ch > 0 || kk > 0) ? 1u : 0u);
+                        tc_mma(dt, da, dl, idesc[j], 1u);
+                    }
                 }
                 tc_commit(&mbar[s]);
             }
@@ -468,7 +490,7 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
         // each store instruction writes four pixels' 128 contiguous bytes
         // instead of 32 pixels' 16.
         {
-            constexpr int BX_CPW = (BX_NCOL / 32) / (BX_THREADS / 128);
+            constexpr int BX_CPW = (L::PCOL / 32) / (BX_THREADS / 128);
             constexpr int SROW = 36;                        // staging row stride (floats)
             static_assert((BX_THREADS / 32) * 32 * SROW * 4 <= 2 * L::STAGE, "staging fits the stages");
             float *stg = reinterpret_cast<float *>(smem) + warp * (32 * SROW);
@@ -527,7 +549,7 @@ __device__ __forceinline__ uint32_t box_setup(unsigned char *smem, BoxPipe &st)
     const int tid = threadIdx.x, warp = tid >> 5;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     :: "r"(smem_addr(tmem_slot)), "r"(BX_NCOL) : "memory");
+                     :: "r"(smem_addr(tmem_slot)), "r"(L::PCOL) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
@@ -569,7 +591,7 @@ __device__ __forceinline__ void box_teardown(unsigned char *smem, uint32_t tbase
     __syncthreads();
     fence_after_sync();
     if (warp == 0) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(BX_NCOL) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(L::PCOL) : "memory");
     }
 }
 
@@ -675,7 +697,9 @@ int gram_box_record(int nb)
     return 8 * (dp * (dp + 1) / 2);
 }
 
-int gram_box_kc(int nb) { return nb <= 32 ? 64 : 32; }
+// samples per chunk: 32 for every depth, so that two accumulators (512
+// Gamma columns per pass) fit beside two operand stages
+int gram_box_kc(int nb) { (void)nb; return 32; }
 
 long long gram_box_tiles(const KParams &P) { return box_tiles(P); }
 
@@ -705,7 +729,7 @@ cudaError_t launch_gram_box(const KParams &P, int num_sms, cudaStream_t st)
     if (!gram_box_supported(P.nb, P.ny, P.nx) || P.cols <= 0 || P.pix_begin % P.cols || P.npix % P.cols)
         return cudaErrorInvalidValue;
     if (P.npix == 0) return cudaSuccess;
-    return (P.nb <= 32) ? launch_box_t<64>(P, num_sms, st) : launch_box_t<32>(P, num_sms, st);
+    return gram_box_kc(P.nb) == 64 ? launch_box_t<64>(P, num_sms, st) : launch_box_t<32>(P, num_sms, st);
 }
 
 }  // namespace fpl

@@ -412,7 +412,7 @@ void fpl_server_config_default(fpl_server_config *c)
     if (!c) return;
     std::memset(c, 0, sizeof(*c));
     c->memory_budget = (size_t)80 << 30;   // 80 GB
-    c->wave_pixels = 1 << 19;
+    c->wave_pixels = 1 << 20;
     c->device = 0;
 }
 

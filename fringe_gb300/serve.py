@@ -17,7 +17,7 @@ from .linker import _make_job
 
 
 class Server:
-    def __init__(self, memory_budget=80 << 30, wave_pixels=1 << 19, device=0):
+    def __init__(self, memory_budget=80 << 30, wave_pixels=1 << 20, device=0):
         self.lib = _lib.load()
         cfg = _lib.FplServerConfig()
         self.lib.fpl_server_config_default(ctypes.byref(cfg))

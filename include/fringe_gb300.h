@@ -186,7 +186,7 @@ int fpl_batch_destroy(fpl_batch *batch);
 typedef struct fpl_server fpl_server;
 typedef struct {
     size_t memory_budget;      /* device bytes for resident jobs (default 80 GB) */
-    long long wave_pixels;     /* pixels per wave (default 524288)              */
+    long long wave_pixels;     /* pixels per wave (default 1048576)             */
     int device;
 } fpl_server_config;
 typedef struct {
