@@ -248,9 +248,9 @@ struct BatchClass {
 // one wave of the mixed-form pieces: Gamma segments per chunk width
 // (index 0: 64 samples, 1: 32) and solve entries per padded depth (16/32/64)
 struct MixedWave {
-    int seg_first[2] = {0, 0}, seg_count[2] = {0, 0};
-    long long seg_tiles[2] = {0, 0};
-    size_t seg_smem[2] = {0, 0};
+    int seg_first = 0, seg_count = 0;
+    long long seg_tiles = 0;
+    size_t seg_smem = 0;
     int ent_first[3] = {0, 0, 0}, ent_count[3] = {0, 0, 0};
     long long ent_total[3] = {0, 0, 0};
 };
@@ -293,14 +293,11 @@ int batch_enqueue(fpl_batch *b, cudaStream_t st)
             cudaSuccess)
             return FPL_ERR_CUDA;
     }
-    static const int kKC[2] = {64, 32};
     static const int kNP[3] = {16, 32, 64};
     for (const MixedWave &w : b->waves) {
-        for (int c = 0; c < 2; ++c)
-            if (w.seg_count[c] && fpl::launch_gram_batch(kKC[c], b->d_segs + w.seg_first[c], w.seg_count[c],
-                                                         w.seg_tiles[c], w.seg_smem[c], ctx->num_sms,
-                                                         st) != cudaSuccess)
-                return FPL_ERR_CUDA;
+        if (w.seg_count && fpl::launch_gram_batch(b->d_segs + w.seg_first, w.seg_count, w.seg_tiles, w.seg_smem,
+                                                  ctx->num_sms, st) != cudaSuccess)
+            return FPL_ERR_CUDA;
         for (int c = 0; c < 3; ++c)
             if (w.ent_count[c] && fpl::launch_solve_batch(kNP[c], b->d_ments + w.ent_first[c], w.ent_count[c],
                                                           w.ent_total[c], ctx->num_sms, st,
@@ -458,25 +455,22 @@ int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fp
             P.cstride = fpl::gram_box_record(jb.nbands);
             b->job_of_entry.push_back(pc.job);
         }
-        // per wave: segments by chunk width, entries by padded depth
+        // per wave: Gamma segments, entries by padded depth
         std::vector<fpl::BoxSeg> segs;
         std::vector<fpl::BatchEntry> ments;
         for (size_t w = 0; w < b->waves.size(); ++w) {
             MixedWave &mw = b->waves[w];
-            for (int c = 0; c < 2; ++c) {
-                const int kc = c == 0 ? 64 : 32;
-                mw.seg_first[c] = (int)segs.size();
-                for (int i = 0; i < np_; ++i) {
-                    if (wave_of[i] != (int)w || fpl::gram_box_kc(pp[i].nb) != kc) continue;
-                    fpl::BoxSeg sg;
-                    sg.P = pp[i];
-                    sg.tile_offset = mw.seg_tiles[c];
-                    mw.seg_tiles[c] += fpl::gram_box_tiles(pp[i]);
-                    mw.seg_smem[c] = std::max(mw.seg_smem[c], fpl::gram_box_smem(pp[i].nb, pp[i].ny, pp[i].nx));
-                    segs.push_back(sg);
-                }
-                mw.seg_count[c] = (int)segs.size() - mw.seg_first[c];
+            mw.seg_first = (int)segs.size();
+            for (int i = 0; i < np_; ++i) {
+                if (wave_of[i] != (int)w) continue;
+                fpl::BoxSeg sg;
+                sg.P = pp[i];
+                sg.tile_offset = mw.seg_tiles;
+                mw.seg_tiles += fpl::gram_box_tiles(pp[i]);
+                mw.seg_smem = std::max(mw.seg_smem, fpl::gram_box_smem(pp[i].nb, pp[i].ny, pp[i].nx));
+                segs.push_back(sg);
             }
+            mw.seg_count = (int)segs.size() - mw.seg_first;
             for (int c = 0; c < 3; ++c) {
                 const int npd = 16 << c;
                 mw.ent_first[c] = (int)ments.size();

@@ -17,8 +17,10 @@
 //       accumulated in FP32 in tensor memory.
 // Each outer product is formed once per tile instead of once for every pixel
 // that uses it.  One thread issues tcgen05.mma (M = 128 pixels, N <= 256
-// Gamma entries, K = 16 samples); the Gamma entries are processed in passes
-// of 256 columns.
+// Gamma entries, K = 16 samples) into one of two tensor-memory accumulators;
+// the Gamma entries are processed in passes of 512 columns, each pass over
+// the tile's samples in chunks of 32 (two operand stages, one CTA barrier
+// per chunk).
 //
 // Column order (the Gamma record read by the eigen kernel): dates padded to an
 // even count and grouped in pairs; block (a, b), a <= b, row-major over the
@@ -48,7 +50,10 @@ namespace {
 
 constexpr int BX_THREADS = 512;                    // 16 warps: the operand build hides latency
 constexpr int BX_TR = 8, BX_TC = 16, BX_M = 128;   // pixel tile (MMA M)
-constexpr int BX_NCOL = 256;                       // Gamma columns per pass (MMA N)
+constexpr int BX_NCOL = 256;                       // Gamma columns per accumulator (MMA N)
+// samples per chunk (MMA K of one stage): 32, so that two accumulators (512
+// Gamma columns per pass) fit beside two operand stages and two sample buffers
+constexpr int BX_KC = 32;
 constexpr int BX_MAXK = 2048;                      // union samples per tile
 constexpr int BX_MAXW = BX_MAXK / 32;              // union mask words per pixel
 constexpr int BX_MAXWX = 63;                       // window width (64-bit row extraction)
@@ -68,13 +73,15 @@ template <int KC> struct BoxLay {
     static constexpr int A_BYTES = (BX_M / 8) * SBO;
     static constexpr int B_BYTES = (PCOL / 8) * SBO;         // one of hi / lo
     static constexpr int STAGE = A_BYTES + 2 * B_BYTES;
-    static constexpr int MAXPAIR = (KC == 64) ? 16 : 32;     // date pairs: 32 or 64 dates
+    static constexpr int MAXPAIR = 32;                       // date pairs: 64 dates
     static constexpr int XRS = KC * 16 + 16;                 // bytes per date-pair row of X
-    static constexpr int X_BYTES = MAXPAIR * XRS;
+    static constexpr int X_BYTES = MAXPAIR * XRS;            // one of two sample buffers
     static constexpr size_t OFF_X = 2 * (size_t)STAGE;
-    static constexpr size_t OFF_MISC = OFF_X + X_BYTES;
-    static constexpr size_t OFF_U = OFF_MISC + BX_MISC;
+    static constexpr size_t OFF_MISC = OFF_X + 2 * (size_t)X_BYTES;
+    static constexpr size_t OFF_LUT = OFF_MISC + BX_MISC;          // 256 x 8 bf16 mask patterns
+    static constexpr size_t OFF_U = OFF_LUT + 256 * 16;
     static constexpr size_t MAX_SMEM = OFF_U + (size_t)BX_M * BX_MAXW * 4;
+    static_assert(MAX_SMEM <= 227 * 1024, "shared memory of one CTA");
 };
 
 // union samples of a tile: (8 + 2 ny) rows of (16 + 2 nx) samples, packed
@@ -198,19 +205,18 @@ struct BoxPipe {
     int blk_dp;         // date pairs the block table was built for
 };
 
-// wait until the MMAs reading stage s are complete; the vote keeps the
-// timeout decision uniform across the CTA
-__device__ __forceinline__ bool box_wait(uint64_t *mbar, BoxPipe &st, int s)
+// this thread's wait for the MMAs of stage s (if any are pending); true if
+// the wait gave up.  Every thread polls the barrier itself, so no CTA
+// barrier is needed before the stage is overwritten.
+__device__ __forceinline__ bool box_poll(uint64_t *mbar, BoxPipe &st, int s)
 {
-    bool late = false;
-    if (st.pend & (1u << s)) {
-        long long spins = 0;
-        while (!mbar_try_wait(&mbar[s], (st.par >> s) & 1u)) {
-            if (++spins > BX_SPIN_LIMIT) { late = true; break; }
-        }
-        if (!late) { st.par ^= 1u << s; st.pend &= ~(1u << s); }
-    }
-    return __syncthreads_or(late) == 0;
+    if (!(st.pend & (1u << s))) return false;
+    long long spins = 0;
+    while (!mbar_try_wait(&mbar[s], (st.par >> s) & 1u))
+        if (++spins > BX_SPIN_LIMIT) return true;
+    st.par ^= 1u << s;
+    st.pend &= ~(1u << s);
+    return false;
 }
 
 // tiles of the rows [ra, rb) of a launch: 8-row tiles on the absolute grid
@@ -234,18 +240,19 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
     unsigned char *Xb = smem + L::OFF_X;
     unsigned char *misc = smem + L::OFF_MISC;
     uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);                 // 2 stages
-    uint32_t *badw = reinterpret_cast<uint32_t *>(misc + 32);            // [2][KC / 32]
     int *pinfo = reinterpret_cast<int *>(misc + 64);                     // 128
     int *pdefer = reinterpret_cast<int *>(misc + 64 + 512);              // 128
     short2 *blk = reinterpret_cast<short2 *>(misc + 64 + 1024);          // <= 528 blocks
+    uint32_t *tbad = reinterpret_cast<uint32_t *>(misc + 3200);          // [W] out-of-range samples
     uint32_t *umask = reinterpret_cast<uint32_t *>(smem + L::OFF_U);     // [128][W]
+    const uint4 *lut = reinterpret_cast<const uint4 *>(smem + L::OFF_LUT);
     uint32_t *nm = reinterpret_cast<uint32_t *>(smem + L::STAGE);        // nmap words (stage 1, mask build only)
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n = P.nb, dp = (n + 1) >> 1, nblk = dp * (dp + 1) / 2, ncolt = 8 * nblk;
     const int cols = P.cols, rows = P.rows, nul = P.nulong;
     const int wy = 2 * P.ny + 1, wx = P.wx;
-    const int uh = BX_TR + wy - 1, uw = BX_TC + wx - 1, uwp = box_union_cols(P.nx);
+    const int uh = BX_TR + wy - 1, uwp = box_union_cols(P.nx);   // union rows, columns
     const int kp = (uh * uwp + KC - 1) / KC * KC, nchunk = kp / KC;
     const int W = kp >> 5;
     const int ra = int(P.pix_begin / cols), rb = ra + int(P.npix / cols);
@@ -267,6 +274,7 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
     }
     // ---- per-pixel SHP masks over the union samples ----------------
     for (int e = tid; e < BX_M * W; e += BX_THREADS) umask[e] = 0;
+    for (int e = tid; e < W; e += BX_THREADS) tbad[e] = 0;
     for (int e = tid; e < BX_M * nul; e += BX_THREADS) {
         const int m = e / nul, w = e - m * nul;
         const int r = R0 + m / BX_TC, c = C0 + m % BX_TC;
@@ -309,57 +317,73 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
             }
         }
         pinfo[m] = info;
-        pdefer[m] = 0;
     }
-    // (the first chunk's barriers order these before any use)
+    // (the prologue's barrier orders these before any use)
 
     // samples of chunk k0 (date pairs interleaved): each thread loads one
-    // sample for up to BX_XPT dates into registers (32 dates at KC = 64,
-    // 64 at KC = 32, over the CTA); put() stores them in Xb and flags
-    // samples outside the split range for the stage's mask.  The loads run
-    // two chunks ahead of the build: chunk c waits in xa (c even) or xb
+    // sample for up to BX_XPT dates into registers (64 dates over the CTA);
+    // put() stores them in one of two sample buffers (chunk g in buffer
+    // g & 1) and flags samples outside the split range in tbad.  The loads
+    // run two chunks ahead of the build: chunk c waits in xa (c even) or xb
     // (c odd), chosen by a branch so both stay in registers, and no copy
     // between them waits for loads in flight.
-    constexpr int BX_XPT = (KC == 64 ? 32 : 64) * KC / BX_THREADS;
-    static_assert(BX_XPT >= 1 && BX_XPT * (BX_THREADS / KC) == (KC == 64 ? 32 : 64), "date coverage");
+    constexpr int BX_XPT = 2 * L::MAXPAIR * KC / BX_THREADS;
+    static_assert(BX_XPT >= 1 && BX_XPT * (BX_THREADS / KC) == 2 * L::MAXPAIR, "date coverage");
     const int sidx = tid % KC, d0 = tid / KC;
     float2 xa[BX_XPT], xb[BX_XPT];
-    auto fetch = [&](int k0, float2 (&xo)[BX_XPT]) {
-        const int k = k0 + sidx;
-        const int ur = k / uwp, uc = k - ur * uwp;
-        const int r = R0 - P.ny + ur, c = C0 - P.nx + uc;
-        const bool valid = uc < uw && ur < uh && r >= 0 && r < rows && c >= 0 && c < cols;
-        const float2 *src = P.stack + (valid ? (long long)r * cols + c : 0ll);
+    // chunks are loaded in cyclic order (0, 1, .., nchunk - 1, 0, ..): the
+    // union row and column of this thread's next sample advance by KC
+    // (< 3 union rows of >= 16 samples) and return to the start after the
+    // last chunk, with no division per chunk
+    const int ur0 = sidx / uwp, uc0 = sidx - ur0 * uwp;
+    int fur = ur0, fuc = uc0, fch = 0;
+    const float2 *sbase = P.stack + (long long)d0 * plane;
+    auto fetch = [&](float2 (&xo)[BX_XPT]) {
+        const int r = R0 - P.ny + fur, c = C0 - P.nx + fuc;
+        const bool valid = fur < uh && r >= 0 && r < rows && c >= 0 && c < cols;
+        const float2 *src = sbase + (valid ? (long long)r * cols + c : 0ll);
 #pragma unroll
         for (int q = 0; q < BX_XPT; ++q) {
             const int d = d0 + q * (BX_THREADS / KC);
             float2 x = make_float2(0.f, 0.f);
-            if (valid && d < n) x = __ldg(src + d * plane);
+            if (valid && d < n) x = __ldg(src + (long long)(q * (BX_THREADS / KC)) * plane);
             xo[q] = x;
         }
+        if (++fch == nchunk) {
+            fch = 0;
+            fur = ur0;
+            fuc = uc0;
+        } else {
+            fuc += KC;
+            if (fuc >= uwp) { fuc -= uwp; ++fur; }
+            if (fuc >= uwp) { fuc -= uwp; ++fur; }
+        }
     };
-    auto put = [&](uint32_t *bw, const float2 (&xv)[BX_XPT]) {
+    // range checks: always in the first pass; in later passes only if the
+    // first found an out-of-range sample in the tile (clean: it found none)
+    bool clean = false;
+    auto put = [&](unsigned char *xd, int k0, const float2 (&xv)[BX_XPT]) {
         bool xbad = false;
 #pragma unroll
         for (int q = 0; q < BX_XPT; ++q) {
             const int d = d0 + q * (BX_THREADS / KC);
             if (d >= 2 * dp) break;
             float2 x = xv[q];
-            if (!split_range(x.x) || !split_range(x.y)) {
+            if (!clean && (!split_range(x.x) || !split_range(x.y))) {
                 xbad = true;
                 x = make_float2(0.f, 0.f);
             }
-            *reinterpret_cast<float2 *>(Xb + (d >> 1) * L::XRS + sidx * 16 + (d & 1) * 8) = x;
+            *reinterpret_cast<float2 *>(xd + (d >> 1) * L::XRS + sidx * 16 + (d & 1) * 8) = x;
         }
-        if (xbad) atomicOr(bw + (sidx >> 5), 1u << (sidx & 31));
+        if (xbad) atomicOr(tbad + ((k0 + sidx) >> 5), 1u << ((k0 + sidx) & 31));
     };
-    // prologue: the first chunk of the tile into Xb (its stage's flags
-    // were cleared when that stage was last used, or at start-up), the
-    // second one into xa
+    static_assert(KC <= 2 * BX_TC, "a chunk advances at most two union rows");
+    // prologue: the first chunk of the tile into buffer 0, the second one
+    // into xb
     const int gtot = npass * nchunk;
-    fetch(0, xa);
-    put(badw + (st.gstep & 1) * (KC / 32), xa);
-    if (gtot > 1) fetch((1 % nchunk) * KC, xb);
+    fetch(xa);
+    put(Xb, 0, xa);
+    if (gtot > 1) fetch(xb);
     __syncthreads();
 
     for (int pass = 0; pass < npass && !st.timed_out; ++pass) {
@@ -376,41 +400,36 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
         }
         for (int ch = 0; ch < nchunk; ++ch) {
             const int s = st.gstep & 1;
-            if (!box_wait(mbar, st, s)) { st.timed_out = true; break; }
+            // the stage's previous MMAs (two chunks back) must be done
+            // before it is overwritten; a thread whose wait gave up builds
+            // nothing and the vote below stops the CTA
+            const bool late = box_poll(mbar, st, s);
             unsigned char *As = smem + s * L::STAGE;
             unsigned char *Bh = As + L::A_BYTES, *Bl = Bh + L::B_BYTES;
-            uint32_t *bw = badw + s * (KC / 32);
             const int k0 = ch * KC;
             // chunk g + 1 (the first chunk again after the last one of a
             // pass) is in registers; chunk g + 2 is loaded while this one
             // is built, into the array chunk g left
             const int g = pass * nchunk + ch;
             const bool more = g + 1 < gtot;
+            const unsigned char *Xc = Xb + (g & 1) * L::X_BYTES;
             if (g + 2 < gtot) {
-                if (g & 1) fetch(((g + 2) % nchunk) * KC, xb);
-                else fetch(((g + 2) % nchunk) * KC, xa);
+                if (g & 1) fetch(xb);
+                else fetch(xa);
             }
-            if (tid < KC / 32) badw[(s ^ 1) * (KC / 32) + tid] = 0;   // for the next chunk
             // ---- A: SHP mask rows ----
-            for (int e = tid; e < BX_M * (KC / 8); e += BX_THREADS) {
+            for (int e = late ? BX_M * (KC / 8) : tid; e < BX_M * (KC / 8); e += BX_THREADS) {
                 const int m = e & (BX_M - 1), k8 = e >> 7;
                 const int b0 = k0 + k8 * 8;
                 const uint32_t bits = (umask[m * W + (b0 >> 5)] >> (b0 & 31)) & 0xffu;
-                const uint32_t bad = (bw[(k8 * 8) >> 5] >> ((k8 * 8) & 31)) & 0xffu;
-                if (bits & bad) pdefer[m] = 1;
-                uint32_t v[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    v[q] = ((bits >> (2 * q)) & 1u ? 0x3F80u : 0u) | ((bits >> (2 * q + 1)) & 1u ? 0x3F800000u : 0u);
-                *reinterpret_cast<uint4 *>(As + (m >> 3) * L::SBO + k8 * 128 + (m & 7) * 16) =
-                    make_uint4(v[0], v[1], v[2], v[3]);
+                *reinterpret_cast<uint4 *>(As + (m >> 3) * L::SBO + k8 * 128 + (m & 7) * 16) = lut[bits];
             }
             // ---- B: outer-product entries, hi and lo ----
             // one thread per half core matrix: block bl's rows 4 ia .. 4 ia + 3
             // (entries (2a + ia, 2b), (2a + ia, 2b + 1), Re and Im) over the 8
             // samples of K group k8
             constexpr int NBL = L::PCOL / 8;                 // column blocks of the pass
-            for (int e = tid; e < 2 * NBL * (KC / 8); e += BX_THREADS) {
+            for (int e = late ? 2 * NBL * (KC / 8) : tid; e < 2 * NBL * (KC / 8); e += BX_THREADS) {
                 const int bl = e % NBL, ia = (e / NBL) & 1, k8 = e / (2 * NBL);
                 const int jacc = bl / (BX_NCOL / 8);
                 const int nm_j = (jacc == 0) ? nmma[0] : nmma[L::NACC - 1];
@@ -427,8 +446,8 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
                     continue;
                 }
                 const short2 ab = blk[cb / 8 + bl];
-                const unsigned char *sa = Xb + ab.x * L::XRS + k8 * 128;
-                const unsigned char *sb = Xb + ab.y * L::XRS + k8 * 128;
+                const unsigned char *sa = Xc + ab.x * L::XRS + k8 * 128;
+                const unsigned char *sb = Xc + ab.y * L::XRS + k8 * 128;
                 float2 pa[8];          // per sample: x_{2a + ia}
                 float4 pb[8];          // per sample: x_{2b}, x_{2b+1}
 #pragma unroll
@@ -449,8 +468,16 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
                     store_split(dh + (2 * jb + 1) * 16, dl + (2 * jb + 1) * 16, im);
                 }
             }
+            // the next chunk's samples go to the other buffer, which the
+            // previous chunk's build (before the previous barrier) read last
+            if (more) {
+                unsigned char *Xn = Xb + ((g + 1) & 1) * L::X_BYTES;
+                const int kn = ((g + 1) % nchunk) * KC;
+                if (g & 1) put(Xn, kn, xa);
+                else put(Xn, kn, xb);
+            }
             fence_async_smem();
-            __syncthreads();
+            if (__syncthreads_or(late)) { st.timed_out = true; break; }
             if (tid == 0) {
                 fence_after_sync();
                 const uint32_t a0 = smem_addr(As), h0 = smem_addr(Bh), l0 = smem_addr(Bl);
@@ -472,17 +499,25 @@ __device__ void box_tile(const KParams &P, long long t, unsigned char *smem, uin
             }
             st.pend |= 1u << s;
             ++st.gstep;
-            // every thread has finished building this chunk (barrier
-            // above): the prefetched samples replace it in Xb; the next
-            // iteration's wait is the barrier before they are read
-            if (more) {
-                if (g & 1) put(badw + (s ^ 1) * (KC / 32), xa);
-                else put(badw + (s ^ 1) * (KC / 32), xb);
-            }
         }
         if (st.timed_out) return;
-        if (!box_wait(mbar, st, 0) || !box_wait(mbar, st, 1)) { st.timed_out = true; break; }
+        const bool late = box_poll(mbar, st, 0) || box_poll(mbar, st, 1);
+        if (pass == 0 && tid < BX_M) {
+            // every sample of the tile has been stored (the last one before
+            // the last chunk's barrier): a pixel with an out-of-range SHP
+            // sample goes to the FP64 path
+            const int m = tid;
+            uint32_t hit = 0;
+            for (int w = 0; w < W; ++w) hit |= umask[m * W + w] & tbad[w];
+            pdefer[m] = hit != 0;
+        }
+        if (__syncthreads_or(late)) { st.timed_out = true; break; }
         fence_after_sync();
+        if (pass == 0) {
+            uint32_t any = 0;
+            for (int w = 0; w < W; ++w) any |= tbad[w];
+            clean = any == 0;
+        }
         // ---- epilogue: warp w reads TMEM lanes 32(w%4).., BX_CPW x 32 columns ----
         // A lane holds its own pixel's columns; they are written out through
         // a 32 x 32 staging tile per warp (in the operand stages, which no
@@ -545,7 +580,6 @@ __device__ __forceinline__ uint32_t box_setup(unsigned char *smem, BoxPipe &st)
     unsigned char *misc = smem + L::OFF_MISC;
     uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(misc + 16);
-    uint32_t *badw = reinterpret_cast<uint32_t *>(misc + 32);
     const int tid = threadIdx.x, warp = tid >> 5;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -557,7 +591,15 @@ __device__ __forceinline__ uint32_t box_setup(unsigned char *smem, BoxPipe &st)
         mbar_init(&mbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (tid < 2 * (KC / 32)) badw[tid] = 0;
+    // mask patterns: entry b holds 8 bf16 values, 1 where bit q of b is set
+    uint4 *lut = reinterpret_cast<uint4 *>(smem + L::OFF_LUT);
+    for (int b = tid; b < 256; b += BX_THREADS) {
+        uint32_t v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            v[q] = ((b >> (2 * q)) & 1 ? 0x3F80u : 0u) | ((b >> (2 * q + 1)) & 1 ? 0x3F800000u : 0u);
+        lut[b] = make_uint4(v[0], v[1], v[2], v[3]);
+    }
     st.pend = 0;
     st.par = 0;
     st.gstep = 0;
@@ -697,31 +739,24 @@ int gram_box_record(int nb)
     return 8 * (dp * (dp + 1) / 2);
 }
 
-// samples per chunk: 32 for every depth, so that two accumulators (512
-// Gamma columns per pass) fit beside two operand stages
-int gram_box_kc(int nb) { (void)nb; return 32; }
-
 long long gram_box_tiles(const KParams &P) { return box_tiles(P); }
 
 size_t gram_box_smem(int nb, int ny, int nx)
 {
-    return gram_box_kc(nb) == 64 ? box_smem<64>(ny, nx) : box_smem<32>(ny, nx);
+    (void)nb;
+    return box_smem<BX_KC>(ny, nx);
 }
 
 cudaError_t prepare_gram_batch()
 {
-    cudaError_t e = box_configure(k_gram_batch<64>, BoxLay<64>::MAX_SMEM, box_flags<64, true>());
-    if (e == cudaSuccess) e = box_configure(k_gram_batch<32>, BoxLay<32>::MAX_SMEM, box_flags<32, true>());
-    return e;
+    return box_configure(k_gram_batch<BX_KC>, BoxLay<BX_KC>::MAX_SMEM, box_flags<BX_KC, true>());
 }
 
-cudaError_t launch_gram_batch(int kc, const BoxSeg *segs, int nseg, long long total, size_t smem, int num_sms,
+cudaError_t launch_gram_batch(const BoxSeg *segs, int nseg, long long total, size_t smem, int num_sms,
                               cudaStream_t st)
 {
     if (nseg <= 0 || total <= 0) return cudaSuccess;
-    if (kc == 64) return launch_box_batch_t<64>(segs, nseg, total, smem, num_sms, st);
-    if (kc == 32) return launch_box_batch_t<32>(segs, nseg, total, smem, num_sms, st);
-    return cudaErrorInvalidValue;
+    return launch_box_batch_t<BX_KC>(segs, nseg, total, smem, num_sms, st);
 }
 
 cudaError_t launch_gram_box(const KParams &P, int num_sms, cudaStream_t st)
@@ -729,7 +764,7 @@ cudaError_t launch_gram_box(const KParams &P, int num_sms, cudaStream_t st)
     if (!gram_box_supported(P.nb, P.ny, P.nx) || P.cols <= 0 || P.pix_begin % P.cols || P.npix % P.cols)
         return cudaErrorInvalidValue;
     if (P.npix == 0) return cudaSuccess;
-    return gram_box_kc(P.nb) == 64 ? launch_box_t<64>(P, num_sms, st) : launch_box_t<32>(P, num_sms, st);
+    return launch_box_t<BX_KC>(P, num_sms, st);
 }
 
 }  // namespace fpl

@@ -34,15 +34,13 @@ cudaError_t launch_gram_box(const KParams &P, int num_sms, cudaStream_t st);
 // mixed form: eigen-solves and outputs from P.cbuf / P.cinfo
 cudaError_t launch_solve(const KParams &P, int num_sms, cudaStream_t st);
 
-// batched mixed form.  Launches of one Gamma kernel share its sample-chunk
-// width (gram_box_kc: 64 for <= 32 dates, 32 above); one launch covers
-// gram_box_tiles(P) tiles and needs gram_box_smem bytes of shared memory.
-int gram_box_kc(int nb);
+// batched mixed form: a launch of the Gamma kernel covers gram_box_tiles(P)
+// tiles and needs gram_box_smem bytes of shared memory.
 long long gram_box_tiles(const KParams &P);
 size_t gram_box_smem(int nb, int ny, int nx);
 // tiles of every segment in one persistent launch (smem: the largest
 // gram_box_smem of the segments)
-cudaError_t launch_gram_batch(int kc, const BoxSeg *segs, int nseg, long long total, size_t smem,
+cudaError_t launch_gram_batch(const BoxSeg *segs, int nseg, long long total, size_t smem,
                               int num_sms, cudaStream_t st);
 // kernel attributes of the batched mixed form for padded depth np (call
 // before capturing a launch sequence)

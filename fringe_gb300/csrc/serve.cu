@@ -254,23 +254,21 @@ bool run_wave(fpl_server *s, std::vector<Piece> &pieces)
         coff += P.npix;
         loff += P.npix;
     }
-    // Gamma segments of the mixed pieces, by chunk width (64 samples, then 32)
-    int nseg[2] = {0, 0};
-    long long tiles[2] = {0, 0};
-    size_t gsm[2] = {0, 0};
-    for (int c = 0; c < 2; ++c)
-        for (size_t e = 0; e < pieces.size(); ++e) {
-            const fpl::KParams &P = s->h_table[e].P;
-            if (!pieces[e].mixed || fpl::gram_box_kc(P.nb) != (c == 0 ? 64 : 32)) continue;
-            fpl::BoxSeg &sg = s->h_segs[nseg[0] + nseg[1]];
-            sg.P = P;
-            sg.tile_offset = tiles[c];
-            tiles[c] += fpl::gram_box_tiles(P);
-            gsm[c] = std::max(gsm[c], fpl::gram_box_smem(P.nb, P.ny, P.nx));
-            ++nseg[c];
-        }
-    if (nseg[0] + nseg[1] &&
-        cudaMemcpyAsync(s->d_segs, s->h_segs, sizeof(fpl::BoxSeg) * (nseg[0] + nseg[1]), cudaMemcpyHostToDevice,
+    // Gamma segments of the mixed pieces
+    int nseg = 0;
+    long long tiles = 0;
+    size_t gsm = 0;
+    for (size_t e = 0; e < pieces.size(); ++e) {
+        const fpl::KParams &P = s->h_table[e].P;
+        if (!pieces[e].mixed) continue;
+        fpl::BoxSeg &sg = s->h_segs[nseg++];
+        sg.P = P;
+        sg.tile_offset = tiles;
+        tiles += fpl::gram_box_tiles(P);
+        gsm = std::max(gsm, fpl::gram_box_smem(P.nb, P.ny, P.nx));
+    }
+    if (nseg &&
+        cudaMemcpyAsync(s->d_segs, s->h_segs, sizeof(fpl::BoxSeg) * nseg, cudaMemcpyHostToDevice,
                         s->s_compute) != cudaSuccess)
         return false;
     if (cudaMemcpyAsync(s->d_table, s->h_table, sizeof(fpl::BatchEntry) * pieces.size(), cudaMemcpyHostToDevice,
@@ -279,11 +277,7 @@ bool run_wave(fpl_server *s, std::vector<Piece> &pieces)
     if (cudaMemsetAsync(s->d_wave, 0, kPieceCounterBytes * s->max_pieces + 64, s->s_compute) != cudaSuccess)
         return false;
     unsigned long long *work = reinterpret_cast<unsigned long long *>(base + kPieceCounterBytes * s->max_pieces);
-    if (nseg[0] && fpl::launch_gram_batch(64, s->d_segs, nseg[0], tiles[0], gsm[0], s->num_sms, s->s_compute) !=
-                       cudaSuccess)
-        return false;
-    if (nseg[1] && fpl::launch_gram_batch(32, s->d_segs + nseg[0], nseg[1], tiles[1], gsm[1], s->num_sms,
-                                          s->s_compute) != cudaSuccess)
+    if (nseg && fpl::launch_gram_batch(s->d_segs, nseg, tiles, gsm, s->num_sms, s->s_compute) != cudaSuccess)
         return false;
     size_t e = 0;
     int cls = 0;

@@ -96,11 +96,13 @@ def test_mixed_row_range(gpu_lib):
     assert not np.any(part["tcorr"][:5]) and not np.any(part["tcorr"][30:])
 
 
-def test_mixed_out_of_range_samples(gpu_lib):
+@pytest.mark.parametrize("nb", [10, 40])
+def test_mixed_out_of_range_samples(gpu_lib, nb):
     """NaN samples, and magnitudes outside the bf16 split's range, send the
     pixels whose SHPs include them to the FP64 path; other pixels of the same
-    tile are unaffected."""
-    stack, nmap = synth.scene("uniform", 24, 40, 10, 2, 3, seed=77)
+    tile are unaffected.  At 40 dates a tile takes four passes over its
+    samples, and the hand-off found in the first pass holds for all four."""
+    stack, nmap = synth.scene("uniform", 24, 40, nb, 2, 3, seed=77)
     stack[2, 5, 7] = np.nan
     stack[:, 15, 30] = 3e17
     stack[4, 20, 3] = 1e-17 + 1e-17j
