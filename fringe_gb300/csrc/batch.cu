@@ -13,7 +13,7 @@
 // Jobs in the mixed-precision form (fpl_job::precision = FPL_PREC_MIXED) are
 // cut into row pieces and packed into waves of at most 2^20 pixels; a wave
 // is one persistent tensor-core Gamma launch over the tiles of all its
-// pieces (per sample-chunk width) and one persistent solve launch over all
+// pieces and one persistent solve launch over all
 // its pixels (per padded depth), the Gamma records staying in a buffer
 // sized for one wave.  Their FP64 settle runs with the FP32 jobs' at the end.
 //
@@ -245,8 +245,8 @@ struct BatchClass {
     int warps = 0;                  // CTA shape
 };
 
-// one wave of the mixed-form pieces: Gamma segments per chunk width
-// (index 0: 64 samples, 1: 32) and solve entries per padded depth (16/32/64)
+// one wave of the mixed-form pieces: its Gamma segments and its solve
+// entries per padded depth (16/32/64)
 struct MixedWave {
     int seg_first = 0, seg_count = 0;
     long long seg_tiles = 0;

@@ -89,7 +89,7 @@ struct fpl_server {
     cudaEvent_t ev_wave = nullptr;
     int max_pieces = 256;
     fpl::BatchEntry *d_table = nullptr, *h_table = nullptr;
-    fpl::BoxSeg *d_segs = nullptr, *h_segs = nullptr;   // mixed pieces of a wave, by chunk width
+    fpl::BoxSeg *d_segs = nullptr, *h_segs = nullptr;   // Gamma segments of a wave's mixed pieces
     void *d_rec = nullptr;                              // their Gamma records and tile infos
     size_t rec_cap = 0;
     void *d_wave = nullptr;
