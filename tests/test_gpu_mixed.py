@@ -38,6 +38,21 @@ def test_mixed_large_window_chunks(gpu_lib):
     assert_parity(compare(g, o), phase_tol=1e-3, tcorr_tol=2e-4)
 
 
+@pytest.mark.parametrize("ny,nx", [(3, 0), (0, 3), (1, 1), (7, 0)])
+def test_mixed_thin_windows(gpu_lib, ny, nx):
+    """Windows one column or one row wide.  With Nx = 0 a union row of a
+    tile holds 16 samples, so each 32-sample chunk of the Gamma kernel spans
+    two whole union rows."""
+    from fringe_gb300 import phase_link
+    stack, nmap = synth.scene("voronoi", 24, 40, 6, ny, nx, seed=31 + ny + nx)
+    for method in ("MLE", "EVD"):
+        g = phase_link(stack, nmap, (ny, nx), method=method, precision="mixed")
+        o = oracle.run(stack, nmap, ny, nx, method=method)
+        m = compare(g, o)
+        assert m["valid_both"] > 0, m
+        assert_parity(m, phase_tol=1e-3, tcorr_tol=2e-4)
+
+
 def _mixed_and_oracle(stack, nmap, ny, nx, **kw):
     from fringe_gb300 import phase_link
     g = phase_link(stack, nmap, (ny, nx), precision="mixed", want_status=True, **kw)
@@ -48,8 +63,9 @@ def _mixed_and_oracle(stack, nmap, ny, nx, **kw):
 
 @pytest.mark.parametrize("nb", [1, 2, 5, 16, 17, 33, 64])
 def test_mixed_depths(gpu_lib, nb):
-    """Every stack depth: odd counts pad the date pairs, more than 32 dates
-    take the 32-sample chunk layout."""
+    """Every stack depth: odd counts pad the date pairs; from 21 dates on a
+    tile's Gamma takes more than one pass (512 columns per pass) over its
+    samples."""
     stack, nmap = synth.scene("voronoi", 20, 24, nb, 2, 3, seed=100 + nb)
     for method, sem in (("MLE", "evd"), ("EVD", "evd"), ("MLE", "phase_link")):
         g, o = _mixed_and_oracle(stack, nmap, 2, 3, method=method, semantics=sem)
