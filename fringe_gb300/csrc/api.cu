@@ -15,6 +15,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "fringe_gb300.h"
 #include "ctx.h"
@@ -373,6 +375,9 @@ int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream)
                        job->status, st, ctx->force_fp64, ctx->d_small, true);
 }
 
+// host threads that put the FP64-settled pixels in place after a host-memory run
+constexpr int kScatterThreads = 8;
+
 // Host-memory jobs run in row chunks so that copies overlap the compute:
 // chunk c's stack rows (with the window apron and the rows of its first and
 // last 8-row tiles) and nmap rows go up on a copy stream, the chunk is
@@ -518,19 +523,40 @@ int fpl_run(fpl_ctx *ctx, const fpl_job *job)
         // are put in place over them
         FPL_CUDA(ctx, cudaStreamSynchronize(ctx->s_out));
         if (nset > 0 && !ctx->force_fp64) {
+            // each settled pixel writes one value into each of nb planes far
+            // apart, so the loop waits on cache misses: split it over host
+            // threads (pixels appear once in the list, so the ranges write
+            // disjoint places)
             float2 *h_phase = static_cast<float2 *>(job->phase), *h_comp = static_cast<float2 *>(job->comp);
-            for (long long e = 0; e < nset; ++e) {
-                const float2 *v = ctx->h_pack.data() + (size_t)e * (nb + 3);
-                uint32_t lo, hi;
-                int32_t stv;
-                std::memcpy(&lo, &v[nb + 2].x, 4);
-                std::memcpy(&hi, &v[nb + 2].y, 4);
-                std::memcpy(&stv, &v[nb + 1].y, 4);
-                const long long pp = (long long)(((uint64_t)hi << 32) | lo);
-                for (int b = 0; b < nb; ++b) h_phase[(size_t)b * plane + pp] = v[b];
-                h_comp[pp] = v[nb];
-                job->tcorr[pp] = v[nb + 1].x;
-                if (job->status) job->status[pp] = stv;
+            const float2 *pack = ctx->h_pack.data();
+            auto put = [&](long long e0, long long e1) {
+                for (long long e = e0; e < e1; ++e) {
+                    const float2 *v = pack + (size_t)e * (nb + 3);
+                    uint32_t lo, hi;
+                    int32_t stv;
+                    std::memcpy(&lo, &v[nb + 2].x, 4);
+                    std::memcpy(&hi, &v[nb + 2].y, 4);
+                    std::memcpy(&stv, &v[nb + 1].y, 4);
+                    const long long pp = (long long)(((uint64_t)hi << 32) | lo);
+                    for (int b = 0; b < nb; ++b) h_phase[(size_t)b * plane + pp] = v[b];
+                    h_comp[pp] = v[nb];
+                    job->tcorr[pp] = v[nb + 1].x;
+                    if (job->status) job->status[pp] = stv;
+                }
+            };
+            const long long per_thread = 512;
+            const int nt = (int)std::max<long long>(
+                1, std::min<long long>({(long long)kScatterThreads, (long long)std::thread::hardware_concurrency(),
+                                        (nset + per_thread - 1) / per_thread}));
+            if (nt <= 1) {
+                put(0, nset);
+            } else {
+                std::vector<std::thread> pool;
+                const long long step = (nset + nt - 1) / nt;
+                for (int t = 1; t < nt; ++t)
+                    pool.emplace_back(put, std::min(nset, t * step), std::min(nset, (t + 1) * step));
+                put(0, std::min(nset, step));
+                for (std::thread &th : pool) th.join();
             }
         }
     }

@@ -248,3 +248,23 @@ def test_scene_past_32_bit_indices(gpu_lib):
     out = phase_link(d_stack, d_nmap, (ny, nx), precision="fp32", rows=(r0, R))
     t = out["tcorr"][r0:, (TC - 1) * B:].cpu().numpy()[inner]
     assert np.array_equal(t, ref_fp32["tcorr"][inner], equal_nan=True)
+
+
+def test_host_run_with_many_settled_pixels_equals_device_run(gpu_lib):
+    """A host-memory run puts the FP64-settled pixels in place on the host,
+    split over several threads once there are more than 512 of them; its
+    outputs equal those of the device-memory run bit for bit."""
+    torch = pytest.importorskip("torch")
+    from fringe_gb300 import _lib, phase_link
+    stack, nmap = synth.scene("illcond", 320, 320, 64, 5, 10, seed=1003)
+    ctx = _lib.Context(0)
+    host = phase_link(stack, nmap, (5, 10), method="MLE", precision="mixed", want_status=True, ctx=ctx)
+    settled = ctx.stats()["fp64_pixels"]
+    assert settled > 2 * 512, settled
+    ts = torch.from_numpy(stack).cuda()
+    tn = torch.from_numpy(nmap.view(np.int32)).cuda()
+    dev = phase_link(ts, tn, (5, 10), method="MLE", precision="mixed", want_status=True, ctx=ctx)
+    torch.cuda.synchronize()
+    assert ctx.stats()["fp64_pixels"] == settled
+    for key in ("phase", "tcorr", "comp", "status"):
+        assert np.array_equal(dev[key].cpu().numpy().view(np.uint8), host[key].view(np.uint8)), key
