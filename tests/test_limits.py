@@ -49,7 +49,13 @@ def test_validation_rejects_before_any_device_work(kw, code):
 
 def test_largest_window_is_accepted_by_validation():
     """31 x 33 = 1023 taps (32 mask words) passes validation; with no GPU the
-    call then fails at its first CUDA call, not at validation."""
+    call then fails at its first CUDA call, not at validation.  The job's
+    buffers are placeholders, so the test runs only where no GPU is visible
+    (with one the call would launch kernels on them); the GPU tests below
+    run that window size on real buffers."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("placeholder buffers: runs only where no GPU is visible")
     lib = _lib.load()
     rc = lib.fpl_run_noalloc(ctypes.byref(_job(ny=15, nx=16)), None)
     assert rc not in (CODES["FPL_ERR_UNSUPPORTED"], CODES["FPL_ERR_OPTIONS"])
