@@ -16,18 +16,25 @@
 //                (nonzero, not NaN, optional input mask), and an ascending
 //                bitonic sort in registers; sorted amplitudes are written
 //                date-planar [N][pixel].
-//   k_nmap_ks    (CTA per 32-column x TR-row tile): the sorted amplitudes of
-//                the tile and its window apron are staged in shared memory;
-//                each thread walks its pixel's taps and, for each valid
-//                neighbour, merges the two sorted samples to obtain the KS
+//   k_nmap_fwd<0> (CTA per 32-column x TR-row tile): the sorted amplitudes
+//                of the tile and of the window rows below and beside it are
+//                staged in shared memory; each thread tests its pixel
+//                against the neighbours of the forward half window (the
+//                offsets of the reference's loop, src/nmap/nmap.cpp:399-416:
+//                rows 0..Ny below, and on its own row the columns right of
+//                it), merging the two sorted samples to obtain the KS
 //                statistic D (in steps of 1/N; a run of equal values in both
 //                samples is one step, as in the reference).  The probability
 //                depends on D alone, so the decision is a table lookup
 //                prepared on the host with the reference's Kolmogorov
-//                series.  The test is symmetric, so testing every neighbour
-//                of every pixel gives the reference's half-window-and-mirror
-//                map exactly.
-//   k_nmap_tile<AD2> the same tile walk with the two-sample Anderson-Darling
+//                series.  The results go to a bit array, one bit per pixel
+//                and forward offset.
+//   k_nmap_mirror (thread per pixel): the map as the reference sets it
+//                (nmap.cpp:447-462): a pixel's forward bits are its own
+//                tests, its backward bits those of the neighbour whose
+//                forward offset reaches it; the count is their sum.  Each
+//                pair is tested once.
+//   k_nmap_fwd<1> the same forward tests with the two-sample Anderson-Darling
 //                test (src/nmap/AD2unique.hpp:270-347).  The statistic is a
 //                sum over the merged walk, (2n m_j - n(j+1))^2 /
 //                ((j+1)(2n-j-1)) for the j+1 first values of which m_j come
@@ -38,9 +45,9 @@
 //                a margin far above its rounding; otherwise it repeats the
 //                reference's own FP64 sum, operation for operation, and
 //                compares that with S*.  Ties are merged second sample
-//                first, so the test is not symmetric: every pair is tested
-//                with the reference's first sample, the pixel whose half-
-//                window loop (src/nmap/nmap.cpp:399-416) reaches the other.
+//                first, so the test is not symmetric: like the reference,
+//                each pair is tested with the pixel whose forward half
+//                window reaches the other as the first sample.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -63,6 +70,7 @@ struct NmapParams {
     float *sorted;                   // [nb][rows*cols]
     uint8_t *valid;                  // [rows*cols]
     uint32_t *nmap;                  // [rows*cols][nulong]
+    uint32_t *fwd;                   // [rows*cols][fw]: forward half-window results
     int32_t *count;                  // optional [rows*cols]
     double alpha[FPL_MAX_BANDS];     // normalised calibration constants
     unsigned long long pass_lo;      // KS2: bit k (k < 64): D = k passes the threshold
@@ -72,7 +80,7 @@ struct NmapParams {
     int ad_mode;                     // AD2: 0 compare, 1 every pair passes, 2 none does
     float ad_w[2 * FPL_MAX_BANDS];   // AD2: n^2 / ((j+1)(2n-j-1)), j < 2n - 1
     long long plane;
-    int rows, cols, nb, ny, nx, nulong, tr;
+    int rows, cols, nb, ny, nx, nulong, tr, fw;
     int unit_alpha;                  // all constants 1: no division
 };
 
@@ -194,10 +202,12 @@ __device__ double ad_walk_exact(const float *A, const float *B, int st, int n)
 }
 
 template <int AD2>
-__global__ void __launch_bounds__(256) k_nmap_tile(NmapParams P)
+__global__ void __launch_bounds__(256) k_nmap_fwd(NmapParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int HW = NM_TC + 2 * P.nx, HH = P.tr + 2 * P.ny, HP = HW * HH;
+    // the tile and the window rows below and beside it: forward offsets
+    // reach rows 0..Ny below and columns -Nx..Nx
+    const int HW = NM_TC + 2 * P.nx, HH = P.tr + P.ny, HP = HW * HH;
     // odd stride between dates: lanes whose merge walks sit at different
     // positions spread over the banks
     const int SP = HP | 1;
@@ -209,18 +219,17 @@ __global__ void __launch_bounds__(256) k_nmap_tile(NmapParams P)
     const int ntc = (P.cols + NM_TC - 1) / NM_TC;
     const int R0 = (blockIdx.x / ntc) * P.tr, C0 = (blockIdx.x % ntc) * NM_TC;
     const int tid = threadIdx.x, nth = blockDim.x;
-    // tile + apron: sorted amplitudes and validity
     for (int e = tid; e < HP; e += nth) {
         const int hr = e / HW, hc = e - hr * HW;
-        const int r = R0 - P.ny + hr, c = C0 - P.nx + hc;
-        const bool in = r >= 0 && r < P.rows && c >= 0 && c < P.cols;
+        const int r = R0 + hr, c = C0 - P.nx + hc;
+        const bool in = r < P.rows && c >= 0 && c < P.cols;
         V[e] = in ? P.valid[(long long)r * P.cols + c] : 0;
     }
     for (int e = tid; e < P.nb * HP; e += nth) {
         const int b = e / HP, h = e - b * HP;
         const int hr = h / HW, hc = h - hr * HW;
-        const int r = R0 - P.ny + hr, c = C0 - P.nx + hc;
-        const bool in = r >= 0 && r < P.rows && c >= 0 && c < P.cols;
+        const int r = R0 + hr, c = C0 - P.nx + hc;
+        const bool in = r < P.rows && c >= 0 && c < P.cols;
         S[b * SP + h] = in ? __ldg(P.sorted + b * P.plane + (long long)r * P.cols + c) : 0.f;
     }
     __syncthreads();
@@ -228,19 +237,18 @@ __global__ void __launch_bounds__(256) k_nmap_tile(NmapParams P)
     const int r = R0 + tr, c = C0 + tc;
     if (tr >= P.tr || r >= P.rows || c >= P.cols) return;
     const long long q = (long long)r * P.cols + c;
-    const int wx = 2 * P.nx + 1, K = (2 * P.ny + 1) * wx;
-    uint32_t *out = P.nmap + q * P.nulong;
-    const int hp = (tr + P.ny) * HW + (tc + P.nx);
+    const int wx = 2 * P.nx + 1, K = (2 * P.ny + 1) * wx, fc = P.ny * wx + P.nx;
+    uint32_t *out = P.fwd + q * P.fw;
+    const int hp = tr * HW + (tc + P.nx);
     const bool pv = V[hp] != 0;
-    int cnt = 0;
     uint32_t word = 0;
-    for (int f = 0; f < K; ++f) {
+    int ii = 0, jj = 0;                               // offset of forward tap g = f - fc
+    for (int g = 0; g < K - fc; ++g) {
         if (pv) {
-            const int ii = f / wx - P.ny, jj = f % wx - P.nx;
             const int hq = hp + ii * HW + jj;
             bool set = false;
             if (V[hq]) {
-                if (hq == hp) {
+                if (g == 0) {
                     set = true;                                  // the centre (nmap.cpp:441-445)
                 } else if (!AD2) {
                     const int D = ks_steps(S + hp, S + hq, SP, P.nb);
@@ -248,24 +256,61 @@ __global__ void __launch_bounds__(256) k_nmap_tile(NmapParams P)
                 } else if (P.ad_mode != 0) {
                     set = P.ad_mode == 1;
                 } else {
-                    // the reference's first sample: this pixel when the
-                    // neighbour lies later in its half-window loop
-                    const bool fwd = ii > 0 || (ii == 0 && jj > 0);
-                    const float *A = S + (fwd ? hp : hq), *B = S + (fwd ? hq : hp);
-                    const float sf = ad_walk_fast(A, B, SP, P.nb, W);
+                    // this pixel is the reference's first sample
+                    const float sf = ad_walk_fast(S + hp, S + hq, SP, P.nb, W);
                     if (sf < P.ad_lo) set = true;
                     else if (sf > P.ad_hi) set = false;
-                    else set = ad_walk_exact(A, B, SP, P.nb) <= P.ad_star;
+                    else set = ad_walk_exact(S + hp, S + hq, SP, P.nb) <= P.ad_star;
                 }
             }
-            if (set) {
-                word |= 1u << (f & 31);
-                ++cnt;
-            }
+            if (set) word |= 1u << (g & 31);
+        }
+        if ((g & 31) == 31 || g == K - fc - 1) {
+            out[g >> 5] = word;
+            word = 0;
+        }
+        if (++jj > P.nx) {
+            jj = -P.nx;
+            ++ii;
+        }
+    }
+}
+
+// the map and count of every pixel from the forward results
+__global__ void __launch_bounds__(256) k_nmap_mirror(NmapParams P)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= P.plane) return;
+    const int r = int(q / P.cols), c = int(q - (long long)r * P.cols);
+    const int wx = 2 * P.nx + 1, K = (2 * P.ny + 1) * wx, fc = P.ny * wx + P.nx;
+    uint32_t *out = P.nmap + q * P.nulong;
+    const uint32_t *own = P.fwd + q * P.fw;
+    int cnt = 0;
+    uint32_t word = 0;
+    int ii = -P.ny, jj = -P.nx;                       // offset of tap f
+    for (int f = 0; f < K; ++f) {
+        bool set;
+        if (f >= fc) {
+            const int g = f - fc;
+            set = (__ldg(own + (g >> 5)) >> (g & 31)) & 1u;
+        } else {
+            // the neighbour's forward test at the mirrored offset
+            // (nmap.cpp:459): ii <= 0, so the neighbour is never below
+            const int rq = r + ii, cq = c + jj, g = fc - f;
+            set = rq >= 0 && cq >= 0 && cq < P.cols &&
+                  ((__ldg(P.fwd + ((long long)rq * P.cols + cq) * P.fw + (g >> 5)) >> (g & 31)) & 1u);
+        }
+        if (set) {
+            word |= 1u << (f & 31);
+            ++cnt;
         }
         if ((f & 31) == 31 || f == K - 1) {
             out[f >> 5] = word;
             word = 0;
+        }
+        if (++jj > P.nx) {
+            jj = -P.nx;
+            ++ii;
         }
     }
     if (P.count) P.count[q] = cnt;
@@ -435,14 +480,15 @@ bool ks_table(int n, double prob, unsigned long long *lo, unsigned *hi)
     return true;
 }
 
+// tile rows of k_nmap_fwd and its shared memory: the tile and Ny rows below
 int nm_tile_rows(int nb, int ny, int nx, size_t *smem)
 {
     const int HW = NM_TC + 2 * nx;
     const size_t per_row = (size_t)HW * (sizeof(float) * nb + 1);
     const size_t budget = 200 * 1024;
     int tr = 8;
-    while (tr > 1 && per_row * (tr + 2 * ny) + sizeof(float) * nb > budget) --tr;
-    *smem = per_row * (tr + 2 * ny) + sizeof(float) * nb;        // + the odd-stride pad per date
+    while (tr > 1 && per_row * (tr + ny) + sizeof(float) * nb > budget) --tr;
+    *smem = per_row * (tr + ny) + sizeof(float) * nb;            // + the odd-stride pad per date
     return *smem <= 227 * 1024 ? tr : 0;
 }
 
@@ -502,8 +548,11 @@ extern "C" int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job)
     cudaStream_t st = ctx->stream;
     const size_t b_stack = (size_t)P.plane * P.nb * 8, b_nmap = (size_t)P.plane * nul * 4;
     const size_t b_sorted = ((size_t)P.plane * P.nb * 4 + 255) & ~size_t(255);   // keeps every region 256-aligned
-    // scratch: sorted amplitudes | validity | (host jobs) mask, stack, nmap, count
-    size_t need = b_sorted + ((P.plane + 255) & ~255ll);
+    // scratch: sorted amplitudes | validity | forward results | (host jobs)
+    // mask, stack, nmap, count
+    P.fw = ((K - (P.ny * wx + P.nx)) + 31) / 32;
+    const size_t b_fwd = ((size_t)P.plane * P.fw * 4 + 255) & ~size_t(255);
+    size_t need = b_sorted + ((P.plane + 255) & ~255ll) + b_fwd;
     if (job->memory == FPL_MEM_HOST)
         need += ((b_stack + 255) & ~size_t(255)) + ((b_nmap + 255) & ~size_t(255)) +
                 (((size_t)P.plane * 4 + 255) & ~size_t(255)) + (((size_t)P.plane + 255) & ~size_t(255));
@@ -519,6 +568,8 @@ extern "C" int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job)
     base += b_sorted;
     P.valid = reinterpret_cast<uint8_t *>(base);
     base += (P.plane + 255) & ~255ll;
+    P.fwd = reinterpret_cast<uint32_t *>(base);
+    base += b_fwd;
     auto fail = [&](cudaError_t e, const char *what) {
         ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
         return FPL_ERR_CUDA;
@@ -550,12 +601,14 @@ extern "C" int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job)
     else if (P.nb <= 32) k_nmap_sort<32><<<sblocks, 128, 0, st>>>(P);
     else k_nmap_sort<64><<<sblocks, 128, 0, st>>>(P);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_sort");
-    auto kern = ad2 ? k_nmap_tile<1> : k_nmap_tile<0>;
+    auto kern = ad2 ? k_nmap_fwd<1> : k_nmap_fwd<0>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
-        return fail(e, "k_nmap_tile attributes");
+        return fail(e, "k_nmap_fwd attributes");
     const long long ntiles = (long long)((P.cols + NM_TC - 1) / NM_TC) * ((P.rows + P.tr - 1) / P.tr);
     kern<<<(unsigned)ntiles, NM_TC * P.tr, smem, st>>>(P);
-    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_tile");
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_fwd");
+    k_nmap_mirror<<<(unsigned)((P.plane + 255) / 256), 256, 0, st>>>(P);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_mirror");
     if (job->memory == FPL_MEM_HOST) {
         if ((e = cudaMemcpyAsync(job->nmap, P.nmap, b_nmap, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
             return fail(e, "copy nmap");
