@@ -63,6 +63,7 @@ namespace fpl {
 namespace {
 
 constexpr int NM_TC = 32;            // tile columns (one warp per tile row)
+constexpr int NM_MAX_TR = 16;        // tile rows at most (512 threads)
 
 struct NmapParams {
     const float2 *stack;             // [nb][rows][cols]
@@ -202,7 +203,7 @@ __device__ double ad_walk_exact(const float *A, const float *B, int st, int n)
 }
 
 template <int AD2>
-__global__ void __launch_bounds__(256) k_nmap_fwd(NmapParams P)
+__global__ void __launch_bounds__(NM_TC * NM_MAX_TR) k_nmap_fwd(NmapParams P)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     // the tile and the window rows below and beside it: forward offsets
@@ -480,16 +481,35 @@ bool ks_table(int n, double prob, unsigned long long *lo, unsigned *hi)
     return true;
 }
 
-// tile rows of k_nmap_fwd and its shared memory: the tile and Ny rows below
-int nm_tile_rows(int nb, int ny, int nx, size_t *smem)
+// shared memory of a k_nmap_fwd tile of tr rows: the tile and Ny rows below
+size_t nm_tile_smem(int nb, int ny, int nx, int tr)
 {
     const int HW = NM_TC + 2 * nx;
     const size_t per_row = (size_t)HW * (sizeof(float) * nb + 1);
-    const size_t budget = 200 * 1024;
-    int tr = 8;
-    while (tr > 1 && per_row * (tr + ny) + sizeof(float) * nb > budget) --tr;
-    *smem = per_row * (tr + ny) + sizeof(float) * nb;            // + the odd-stride pad per date
-    return *smem <= 227 * 1024 ? tr : 0;
+    return per_row * (tr + ny) + sizeof(float) * nb;             // + the odd-stride pad per date
+}
+
+// tile rows of k_nmap_fwd: the height whose resident warps per SM (CTAs
+// that fit in shared memory times warps per CTA) is largest -- the merge
+// walks are latency-bound -- preferring taller tiles, which share their
+// apron among more pixels.  0 when not even one row fits.
+template <typename K>
+int nm_tile_rows(K kern, int nb, int ny, int nx, size_t *smem)
+{
+    int best = 0, best_warps = 0;
+    for (int tr = 1; tr <= NM_MAX_TR; ++tr) {
+        const size_t sm = nm_tile_smem(nb, ny, nx, tr);
+        if (sm > 227 * 1024) break;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) break;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NM_TC * tr, sm) != cudaSuccess) break;
+        if (per_sm * tr >= best_warps && per_sm > 0) {
+            best_warps = per_sm * tr;
+            best = tr;
+        }
+    }
+    if (best > 0) *smem = nm_tile_smem(nb, ny, nx, best);
+    return best;
 }
 
 }  // namespace
@@ -541,10 +561,11 @@ extern "C" int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job)
         ctx->last_error = "the threshold lies within rounding of the Anderson-Darling p-value for this stack depth";
         return FPL_ERR_OPTIONS;
     }
-    size_t smem = 0;
-    P.tr = nm_tile_rows(P.nb, P.ny, P.nx, &smem);
-    if (P.tr <= 0) return FPL_ERR_UNSUPPORTED;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return FPL_ERR_CUDA;
+    auto kern = ad2 ? k_nmap_fwd<1> : k_nmap_fwd<0>;
+    size_t smem = 0;
+    P.tr = nm_tile_rows(kern, P.nb, P.ny, P.nx, &smem);
+    if (P.tr <= 0) return FPL_ERR_UNSUPPORTED;
     cudaStream_t st = ctx->stream;
     const size_t b_stack = (size_t)P.plane * P.nb * 8, b_nmap = (size_t)P.plane * nul * 4;
     const size_t b_sorted = ((size_t)P.plane * P.nb * 4 + 255) & ~size_t(255);   // keeps every region 256-aligned
@@ -601,7 +622,6 @@ extern "C" int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job)
     else if (P.nb <= 32) k_nmap_sort<32><<<sblocks, 128, 0, st>>>(P);
     else k_nmap_sort<64><<<sblocks, 128, 0, st>>>(P);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_sort");
-    auto kern = ad2 ? k_nmap_fwd<1> : k_nmap_fwd<0>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
         return fail(e, "k_nmap_fwd attributes");
     const long long ntiles = (long long)((P.cols + NM_TC - 1) / NM_TC) * ((P.rows + P.tr - 1) / P.tr);
