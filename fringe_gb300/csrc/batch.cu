@@ -43,8 +43,18 @@ __global__ void k_batch(const BatchEntry *__restrict__ jobs, int njobs, long lon
                         unsigned long long *counter)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    const int warps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *sm = smem + (size_t)warp * Lay<float, NP>::bytes;
+    unsigned char *sm = smem + (size_t)warp * KPixWarp<float, NP>::bytes;
+    // <= 32 dates: the coherence rows in tensor memory (CRowsTmemF)
+    __shared__ uint32_t tslot;
+    uint32_t tbase = 0, taddr = 0;
+    int tcols = 0;
+    if constexpr (CRowsTmemF<float, NP>::value) {
+        tcols = tmem_cols_for(warps, NP);
+        tbase = tmem_alloc_cta(&tslot, warp, (uint32_t)tcols);
+        taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(warp >> 2) * CRowsTmem<NP>::kColsPerWarp;
+    }
     while (true) {
         unsigned long long g = 0;
         if (lane == 0) g = atomicAdd(counter, (unsigned long long)kBatchChunk);
@@ -58,9 +68,10 @@ __global__ void k_batch(const BatchEntry *__restrict__ jobs, int njobs, long lon
                 if (jobs[mid].px_offset <= q) lo = mid; else hi = mid - 1;
             }
             const KParams &P = jobs[lo].P;
-            process_pixel<float, NP>(P, P.pix_begin + (q - jobs[lo].px_offset), sm, lane);
+            process_pixel<float, NP>(P, P.pix_begin + (q - jobs[lo].px_offset), sm, lane, taddr);
         }
     }
+    if constexpr (CRowsTmemF<float, NP>::value) tmem_free_cta(tbase, warp, (uint32_t)tcols);
 }
 
 template <int NP>
@@ -106,7 +117,17 @@ cudaError_t configure(KernelFn k, size_t smem)
 }
 
 template <int NP>
-size_t warp_bytes_f32() { return Lay<float, NP>::bytes; }
+size_t warp_bytes_f32() { return KPixWarp<float, NP>::bytes; }
+
+// shared memory of a k_batch<NP> CTA of `warps` warps: with the coherence
+// rows in tensor memory at least half of it, so that one CTA runs per SM and
+// none waits on a tensor-memory allocation
+template <int NP>
+size_t batch_smem_f32(int warps)
+{
+    const size_t s = KPixWarp<float, NP>::bytes * warps;
+    return CRowsTmemF<float, NP>::value ? std::max<size_t>(s, 112 * 1024 + 1024) : s;
+}
 template <int NP>
 size_t warp_bytes_f64() { return Lay<double, NP>::bytes; }
 
@@ -134,11 +155,12 @@ template <int NP>
 cudaError_t launch_batch_np(const BatchEntry *jobs, int njobs, long long total, unsigned long long *counter,
                             int warps, int num_sms, cudaStream_t st)
 {
-    const size_t smem = Lay<float, NP>::bytes * warps;
+    const size_t smem = batch_smem_f32<NP>(warps);
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<NP>, warps * 32, smem);
     if (e != cudaSuccess) return e;
     per_sm = std::max(per_sm, 1);
+    if (CRowsTmemF<float, NP>::value) per_sm = 1;
     k_batch<NP><<<num_sms * per_sm, warps * 32, smem, st>>>(jobs, njobs, total, counter);
     return cudaGetLastError();
 }
@@ -166,15 +188,15 @@ cudaError_t configure_np(int np)
     cudaError_t e = cudaSuccess;
     switch (np) {
     case 16:
-        e = configure(k_batch<16>, Lay<float, 16>::bytes * max_warps(16, false));
+        e = configure(k_batch<16>, batch_smem_f32<16>(max_warps(16, false)));
         if (e == cudaSuccess) e = configure(k_batch_fp64<16>, Lay<double, 16>::bytes * max_warps(16, true));
         break;
     case 32:
-        e = configure(k_batch<32>, Lay<float, 32>::bytes * max_warps(32, false));
+        e = configure(k_batch<32>, batch_smem_f32<32>(max_warps(32, false)));
         if (e == cudaSuccess) e = configure(k_batch_fp64<32>, Lay<double, 32>::bytes * max_warps(32, true));
         break;
     case 64:
-        e = configure(k_batch<64>, Lay<float, 64>::bytes * max_warps(64, false));
+        e = configure(k_batch<64>, batch_smem_f32<64>(max_warps(64, false)));
         if (e == cudaSuccess) e = configure(k_batch_fp64<64>, Lay<double, 64>::bytes * max_warps(64, true));
         break;
     }

@@ -22,15 +22,22 @@ __global__ void k_pixels(KParams P)
     extern __shared__ __align__(16) unsigned char smem[];
     const int warps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *sm = smem + (size_t)warp * Lay<T, NP>::bytes;
+    unsigned char *sm = smem + (size_t)warp * KPixWarp<T, NP>::bytes;
     const long long gw = (long long)blockIdx.x * warps + warp;
     const long long nw = (long long)gridDim.x * warps;
-    // FP64 at 64 dates: C in tensor memory, one lane quadrant per warp
+    // C in tensor memory: FP64 at 64 dates (one lane quadrant per warp) and
+    // FP32 at <= 32 dates (2*NP columns of the warp's quadrant per warp)
     __shared__ uint32_t tslot;
     uint32_t tbase = 0, taddr = 0;
+    int tcols = 0;
     if constexpr (CInTmem<T, NP>::value) {
-        tbase = tmem_alloc_cta(&tslot, warp, 512);
+        tcols = 512;
+        tbase = tmem_alloc_cta(&tslot, warp, tcols);
         taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
+    } else if constexpr (CRowsTmemF<T, NP>::value) {
+        tcols = tmem_cols_for(warps, NP);
+        tbase = tmem_alloc_cta(&tslot, warp, (uint32_t)tcols);
+        taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(warp >> 2) * CRowsTmem<NP>::kColsPerWarp;
     }
     if (sizeof(T) == 4 || P.fb_list == nullptr) {
         for (long long q = gw; q < P.npix; q += nw) process_pixel<T, NP>(P, P.pix_begin + q, sm, lane, taddr);
@@ -40,19 +47,13 @@ __global__ void k_pixels(KParams P)
         for (long long q = fb_next(P, lane); q < cnt; q = fb_next(P, lane))
             process_pixel<T, NP>(P, P.fb_list[q], sm, lane, taddr);
     }
-    if constexpr (CInTmem<T, NP>::value) tmem_free_cta(tbase, warp, 512);
+    if constexpr (CInTmem<T, NP>::value || CRowsTmemF<T, NP>::value) tmem_free_cta(tbase, warp, (uint32_t)tcols);
 }
 
 // mixed form, second half: eigen-solves from the tensor-core Gamma records.
 // TM: each warp keeps its pixel's coherence rows in tensor memory (2*NP
 // columns of its 32-lane quadrant) instead of shared memory, so a CTA holds
 // about twice as many warps; the kernel issues no MMA.
-__device__ __forceinline__ int tmem_cols_for(int warps, int np)
-{
-    int need = ((warps + 3) / 4) * 2 * np * ((np + 31) / 32), cols = 32;
-    while (cols < need) cols <<= 1;
-    return cols;
-}
 
 // pixel pp of the launch P: record -> coherence rows -> solve and outputs
 template <int NP, typename CP>
@@ -256,7 +257,7 @@ template <typename T, int NP>
 static cudaError_t launch_t(const KParams &P, int num_sms, cudaStream_t st)
 {
     static bool configured[64] = {false};
-    const size_t per_warp = Lay<T, NP>::bytes;
+    const size_t per_warp = KPixWarp<T, NP>::bytes;
     const size_t budget = 224 * 1024;   // of the 227 KB a block may opt into
     int warps = int(budget / per_warp);
     if (warps > 16) warps = 16;
@@ -276,7 +277,11 @@ static cudaError_t launch_t(const KParams &P, int num_sms, cudaStream_t st)
         if (warps > lim) warps = lim;
     }
     if (warps < 1) warps = 1;
-    const size_t smem = per_warp * warps;
+    size_t smem = per_warp * warps;
+    // tensor-memory rows: one CTA per SM (at least half the shared memory),
+    // so a second CTA never waits on a tensor-memory allocation
+    constexpr bool one_cta = CInTmem<T, NP>::value || CRowsTmemF<T, NP>::value;
+    if (one_cta && smem < budget / 2 + 1024) smem = budget / 2 + 1024;
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 64 && !configured[dev]) {
@@ -289,7 +294,7 @@ static cudaError_t launch_t(const KParams &P, int num_sms, cudaStream_t st)
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pixels<T, NP>, warps * 32, smem);
     if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
+    if (per_sm < 1 || one_cta) per_sm = 1;
     long long work = P.npix;
     long long blocks = (long long)num_sms * per_sm;
     long long need = (work + warps - 1) / warps;

@@ -215,6 +215,31 @@ template <typename T, int NP> struct CInTmem {
     static constexpr bool value = sizeof(T) == 8 && NP == 64;
 };
 
+// The plain FP32 form at <= 32 dates keeps C in tensor memory as well (rows
+// as CRowsTmem, as the mixed form's solve does), which halves the slab and
+// raises the warps per SM: Gamma is accumulated in registers in one pass,
+// so C is formed over the gather staging (no longer read by then) and moved
+// to tensor memory before the solve reuses that memory.
+template <typename T, int NP> struct CRowsTmemF {
+    static constexpr bool value = sizeof(T) == 4 && NP <= 32;
+};
+// where the pixel kernels form C in the slab
+template <typename T, int NP> struct CmOffset {
+    static constexpr size_t value = CRowsTmemF<T, NP>::value ? Lay<T, NP>::wm : Lay<T, NP>::cm;
+};
+// tensor-memory columns of a CTA whose warps hold np-date coherence rows
+// (CRowsTmem<np>, four warps per lane quadrant): a power of two >= 32
+__device__ __forceinline__ int tmem_cols_for(int warps, int np)
+{
+    int need = ((warps + 3) / 4) * 2 * np * ((np + 31) / 32), cols = 32;
+    while (cols < need) cols <<= 1;
+    return cols;
+}
+// shared memory per warp of the pixel kernels (k_pixels, k_batch)
+template <typename T, int NP> struct KPixWarp {
+    static constexpr size_t bytes = CRowsTmemF<T, NP>::value ? Lay<T, NP>::bytes_noc : Lay<T, NP>::bytes;
+};
+
 // ------------------------------------------------------------------------
 // Access to the rows of the coherence C.  Lane l owns rows l and l + 32;
 // rows are read and written in chunks of 8 complex entries (columns 8c ..
@@ -1337,7 +1362,8 @@ __device__ int pixel_coherence(const KParams &P, long long pp, unsigned char *sm
     constexpr int NBLK = NBR * NBC - CPR * NBR * (NBR - 1) / 2;
     constexpr int PASSES = (NBLK + 31) / 32;
 
-    C2<T> *Cm = reinterpret_cast<C2<T> *>(sm + L::cm);
+    static_assert(!CRowsTmemF<T, NP>::value || PASSES == 1, "C over the staging needs Gamma in registers");
+    C2<T> *Cm = reinterpret_cast<C2<T> *>(sm + CmOffset<T, NP>::value);
     C2<T> *Wm = reinterpret_cast<C2<T> *>(sm + L::wm);
     float2 *Xs = reinterpret_cast<float2 *>(sm + L::wm);
     T *Xr = reinterpret_cast<T *>(sm + L::xr);
@@ -2072,16 +2098,21 @@ __device__ bool rows_coherence(const KParams &P, long long pp, const C2<float> *
     return true;
 }
 
-// taddr: the warp's tensor-memory rows when CInTmem<T, NP> (C is formed in
-// shared memory, then moved there before the solve reuses that memory)
+// taddr: the warp's tensor-memory rows when CInTmem<T, NP> or
+// CRowsTmemF<T, NP> (C is formed in shared memory, then moved there before
+// the solve reuses that memory)
 template <typename T, int NP>
 __device__ void process_pixel(const KParams &P, long long pp, unsigned char *sm, int lane, uint32_t taddr = 0)
 {
     const int npix = pixel_coherence<T, NP>(P, pp, sm, lane);
     if (npix < 0) return;
-    const C2<T> *Cm = reinterpret_cast<const C2<T> *>(sm + Lay<T, NP>::cm);
+    const C2<T> *Cm = reinterpret_cast<const C2<T> *>(sm + CmOffset<T, NP>::value);
     if constexpr (CInTmem<T, NP>::value) {
         const CRowsTmemD<NP> cp{taddr};
+        rows_from_smem<NP>(cp, Cm, lane);
+        pixel_solve<T, NP>(P, pp, sm, lane, npix, cp);
+    } else if constexpr (CRowsTmemF<T, NP>::value) {
+        const CRowsTmem<NP> cp{taddr};
         rows_from_smem<NP>(cp, Cm, lane);
         pixel_solve<T, NP>(P, pp, sm, lane, npix, cp);
     } else {
