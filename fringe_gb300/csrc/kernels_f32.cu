@@ -48,7 +48,7 @@ cudaError_t prepare_mixed_batch(int np)
 int solve_max_warps(int np)
 {
     switch (np) {
-    case 16: return std::min(32, int((224 * 1024) / Lay<float, 16>::bytes_noc));
+    case 16: return std::min(20, int((224 * 1024) / SolveWarp<16, true>::bytes));
     case 32: return std::min(32, int((224 * 1024) / Lay<float, 32>::bytes_noc));
     case 64: return std::min(8, int((224 * 1024) / Lay<float, 64>::bytes_noc));
     }

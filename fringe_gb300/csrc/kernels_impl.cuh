@@ -13,6 +13,7 @@
 #include <type_traits>
 #include "kernels.h"
 #include "pixel.cuh"
+#include "solve_pair.cuh"
 
 namespace fpl {
 
@@ -53,7 +54,19 @@ __global__ void k_pixels(KParams P)
 // mixed form, second half: eigen-solves from the tensor-core Gamma records.
 // TM: each warp keeps its pixel's coherence rows in tensor memory (2*NP
 // columns of its 32-lane quadrant) instead of shared memory, so a CTA holds
-// about twice as many warps; the kernel issues no MMA.
+// about twice as many warps; the kernel issues no MMA.  At padded order 16 a
+// warp solves two pixels, one per 16-lane half (solve_pair.cuh): two slabs
+// per warp, the rows of both in the warp's 2*NP columns.
+template <int NP, bool TM> struct PairSolve {
+    static constexpr bool value = TM && NP == 16;
+};
+template <int NP, bool TM> struct SolveWarp {
+    static constexpr bool pair = PairSolve<NP, TM>::value;
+    static constexpr size_t bytes =
+        pair ? 2 * Lay<float, NP>::bytes_noc : (TM ? Lay<float, NP>::bytes_noc : Lay<float, NP>::bytes);
+    // warp work items: pixel pairs or pixels
+    static __host__ __device__ long long items(long long px) { return pair ? (px + 1) / 2 : px; }
+};
 
 // pixel pp of the launch P: record -> coherence rows -> solve and outputs
 template <int NP, typename CP>
@@ -88,7 +101,7 @@ __device__ __forceinline__ void solve_loop(long long total, const SRC &src)
     extern __shared__ __align__(16) unsigned char smem[];
     const int warps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr size_t per_warp = TM ? Lay<float, NP>::bytes_noc : Lay<float, NP>::bytes;
+    constexpr size_t per_warp = SolveWarp<NP, TM>::bytes;
     unsigned char *sm = smem + (size_t)warp * per_warp;
     const long long gw = (long long)blockIdx.x * warps + warp;
     const long long nw = (long long)gridDim.x * warps;
@@ -107,6 +120,34 @@ __device__ __forceinline__ void solve_loop(long long total, const SRC &src)
         const CRowsTmem<NP> cp{tbase + ((uint32_t)(32 * (warp & 3)) << 16) +
                                (uint32_t)(warp >> 2) * CRowsTmem<NP>::kColsPerWarp};
         C2<float> *A = reinterpret_cast<C2<float> *>(sm + Lay<float, NP>::wm);
+        if constexpr (PairSolve<NP, TM>::value) {
+            // pixels 2k and 2k+1 on halves 0 and 1; MLE pixels with evd
+            // semantics are solved by the halves together, any other pixel by
+            // the whole warp on its half's slab
+            const int h = lane >> 4;
+            const PairHalf H{lane & 15, h, h ? 0xffff0000u : 0x0000ffffu};
+            const long long npair = (total + 1) >> 1;
+            for (long long k = gw; k < npair; k += nw) {
+                const long long q0 = 2 * k;
+                const bool valid = q0 + h < total;
+                long long pp;
+                const KParams &P = src(valid ? q0 + h : q0, pp);
+                const bool paired = valid && P.method == M_MLE && P.semantics != SEM_PL;
+                if (k + nw < npair && q0 + 2 * nw + h < total) {
+                    long long pn;
+                    const KParams &Pn = src(q0 + 2 * nw + h, pn);
+                    pair_prefetch(Pn, pn, H.hl);
+                }
+                pair_mle(P, pp, sm, cp, H, paired);
+                for (int hh = 0; hh < 2; ++hh) {
+                    if (!__shfl_sync(0xffffffffu, (int)(valid && !paired), 16 * hh)) continue;
+                    long long ph;
+                    const KParams &Ph = src(q0 + hh, ph);
+                    unsigned char *smh = sm + hh * Lay<float, NP>::bytes_noc;
+                    solve_pixel<NP>(Ph, ph, smh, lane, cp, reinterpret_cast<C2<float> *>(smh + Lay<float, NP>::wm));
+                }
+            }
+        } else {
         for (long long q = gw; q < total; q += nw) {
             long long pp;
             const KParams &P = src(q, pp);
@@ -116,6 +157,7 @@ __device__ __forceinline__ void solve_loop(long long total, const SRC &src)
                 prefetch_record(Pn, pn, lane);
             }
             solve_pixel<NP>(P, pp, sm, lane, cp, A);
+        }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
@@ -169,7 +211,7 @@ __global__ void __launch_bounds__((TM && NP <= 32) ? 640 : (TM ? 256 : 512), 1) 
 template <int NP, bool TM, typename K>
 static cudaError_t solve_shape(K kern, int *warps_out, int *per_sm_out, size_t *smem_out, int warps_req = 0)
 {
-    const size_t per_warp = TM ? Lay<float, NP>::bytes_noc : Lay<float, NP>::bytes;
+    const size_t per_warp = SolveWarp<NP, TM>::bytes;
     const size_t budget = 224 * 1024;
     // tensor memory: 512 columns per lane quadrant, CRowsTmem<NP>::kColsPerWarp per warp
     const int cap = TM ? int(4 * (512 / CRowsTmem<NP>::kColsPerWarp)) : 16;
@@ -221,7 +263,7 @@ static cudaError_t launch_solve_t(const KParams &P, int num_sms, cudaStream_t st
     size_t smem = 0;
     if ((e = solve_shape<NP, TM>(k_solve<NP, TM>, &warps, &per_sm, &smem)) != cudaSuccess) return e;
     long long blocks = (long long)num_sms * per_sm;
-    long long need = (P.npix + warps - 1) / warps;
+    long long need = (SolveWarp<NP, TM>::items(P.npix) + warps - 1) / warps;
     if (need < blocks) blocks = need > 0 ? need : 1;
     k_solve<NP, TM><<<(unsigned)blocks, warps * 32, smem, st>>>(P);
     return cudaGetLastError();
@@ -247,7 +289,7 @@ static cudaError_t launch_solve_batch_t(const BatchEntry *ents, int nent, long l
     size_t smem = 0;
     if ((e = solve_shape<NP, TM>(k_solve_batch<NP, TM>, &warps, &per_sm, &smem, warps_req)) != cudaSuccess) return e;
     long long blocks = (long long)num_sms * per_sm;
-    long long need = (total + warps - 1) / warps;
+    long long need = (SolveWarp<NP, TM>::items(total) + warps - 1) / warps;
     if (need < blocks) blocks = need > 0 ? need : 1;
     k_solve_batch<NP, TM><<<(unsigned)blocks, warps * 32, smem, st>>>(ents, nent, total);
     return cudaGetLastError();
