@@ -1242,9 +1242,14 @@ __device__ int warp_inverse_iteration(C2<T> *W, int n, T sigma, unsigned char *s
 // inverse iteration
 constexpr int kPowerStartIters = 2;
 
-template <typename T> struct BlockShape;
-template <> struct BlockShape<float> { static constexpr int BR = 8; };
-template <> struct BlockShape<double> { static constexpr int BR = 4; };
+// register block of the upper triangle of Gamma each lane accumulates
+// (BR rows x BC columns): 8 x 4 in FP32 and 4 x 4 in FP64 give 20 and 36
+// blocks at 32 dates; at 16 dates FP32 uses 4 x 2 blocks, so that 20 lanes
+// share the sums instead of the 6 that 8 x 4 blocks would leave busy
+template <typename T, int NP> struct BlockShape {
+    static constexpr int BR = sizeof(T) == 4 ? (NP <= 16 ? 4 : 8) : 4;
+    static constexpr int BC = (sizeof(T) == 4 && NP <= 16) ? 2 : 4;
+};
 
 template <typename T>
 __device__ __forceinline__ void acc_prod(C2<T> &acc, float2 a, float2 b);
@@ -1356,7 +1361,7 @@ __device__ int pixel_coherence(const KParams &P, long long pp, unsigned char *sm
     using L = Lay<T, NP>;
     constexpr int LD = L::LD;
     constexpr int XS = L::XS;
-    constexpr int BR = BlockShape<T>::BR, BC = 4;
+    constexpr int BR = BlockShape<T, NP>::BR, BC = BlockShape<T, NP>::BC;
     constexpr int NBR = NP / BR, NBC = NP / BC;
     constexpr int CPR = BR / BC;   // first block column of block row R is CPR*R
     constexpr int NBLK = NBR * NBC - CPR * NBR * (NBR - 1) / 2;
