@@ -682,13 +682,16 @@ __device__ int lam_min_test_c(const CP &cp, C2<T> *W, C2<T> *col, int n, T thr, 
 // largest absolute row sum of the inverse.
 // ------------------------------------------------------------------------
 template <typename T, int LD, int NP>
-__device__ bool warp_sweep_inverse(T *A, int n, T *rowk, T *inf_norm, int lane)
+__device__ bool warp_sweep_inverse(T *A, int n, T *rowk, T *inf_norm, int lane, int *kfail = nullptr)
 {
     for (int k = 0; k < n; ++k) {
         for (int j = lane; j < NP; j += 32) rowk[j] = (j < n) ? A[k * LD + j] : T(0);
         __syncwarp();
         const T p = rowk[k];
-        if (!(p > T(0))) return false;
+        if (!(p > T(0))) {
+            if (kfail) *kfail = k;           // rowk holds row k (see abs_not_pd)
+            return false;
+        }
         const T rp = T(1) / p;
         for (int i = lane; i < n; i += 32) {
             T *__restrict__ Ai = A + i * LD;
@@ -743,7 +746,8 @@ __device__ bool warp_sweep_inverse(T *A, int n, T *rowk, T *inf_norm, int lane)
 // for every k), which keeps the code small.  rowb: 2 x NP + 2 floats of
 // shared memory (16-byte aligned): two row buffers and two pivot slots.
 template <int LD, int NP>
-__device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf_norm, int lane)
+__device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf_norm, int lane,
+                                        int *kfail = nullptr)
 {
     static_assert(NP <= 32 && NP % 8 == 0, "one row per lane");
     float x[NP];
@@ -768,7 +772,10 @@ __device__ bool warp_sweep_inverse_rows(float *A, int n, float *rowb, float *inf
         }
         __syncwarp();
         const float p = *pk;
-        if (!(p > 0.f)) return false;
+        if (!(p > 0.f)) {
+            if (kfail) *kfail = k;           // rk holds row k, entries j < k (see abs_not_pd)
+            return false;
+        }
         const float rp = 1.f / p;
         const bool own = (lane == k);
         // row k: a_kj / p;  other rows: a_ij - (a_ik / p) a_kj  (a_ik = a_ki)
@@ -1235,6 +1242,93 @@ __device__ int warp_inverse_iteration(C2<T> *W, int n, T sigma, unsigned char *s
     return 0;
 }
 
+// power steps that refine the vector of the not-positive-definite proof
+constexpr int kNotPdSteps = 2;
+
+// |C| not positive definite, proved from a failed sweep of |C|.  When the
+// sweep meets the pivot p <= 0 at step k, the entries w_j (j < k) of row k
+// solve |C|_SS w = |C|_Sk over the swept indices S, and v = (-w, 1, 0, ..)
+// has v^T |C| v = p in exact arithmetic.  The form is evaluated again from
+// the coherence rows (|C| formed as the sweep formed it): a value below
+// -(g s + band |v|^2), with s = |v|^T |C| |v| and g its evaluation's
+// rounding bound, and band the bound on the spectral difference from the
+// reference's |C| that the other decisions use, proves that the reference's
+// |C| has a negative eigenvalue (any vector serves as the witness).  When v
+// falls short, up to kNotPdSteps power steps on ||C||_inf I - |C| move it
+// toward the eigenvector of the smallest eigenvalue and the test is taken
+// again.  rk: row k (entries j < k are read); amb: the band per unit of
+// ||C||_F, whose sum is taken in the first pass; ub: NP entries of scratch.
+// Every lane calls it.
+template <typename T, int NP, typename CP>
+__device__ bool abs_not_pd(const CP &cp, const T *rk, int k, int n, T amb, T *ub, int lane)
+{
+    constexpr bool fp32 = sizeof(T) == 4;
+    constexpr int H = RowShape<NP>::H;
+    for (int i = lane; i < NP; i += 32) ub[i] = (i < k) ? -rk[i] : (i == k ? T(1) : T(0));
+    __syncwarp();
+    const T g = T(2 * (n + 1)) * Eps<T>::v;
+    T band = T(0), anorm = T(0);
+    for (int it = 0;; ++it) {
+        T q = T(0), s = T(0), v2 = T(0), f2 = T(0), rmax = T(0);
+        T u[H];
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            const int i = lane + 32 * h;
+            const T vi = (i < n) ? ub[i] : T(0);
+            T yq = T(0), ys = T(0), rs = T(0);
+#pragma unroll 1
+            for (int c = 0; c < RowShape<NP>::CH; ++c) {
+                C2<T> cv[8];
+                cp.load(h, c, cv);
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) {
+                    const int j = 8 * c + kk;
+                    if (i >= n || j >= n) continue;
+                    const T m2 = cabs2(cv[kk]);
+                    f2 += m2;
+                    const T a = (i == j) ? T(1) : (fp32 ? m2 * rsqrt_t(max(m2, T(1e-37))) : sqrt(m2));
+                    const T vj = ub[j];
+                    yq = fma(a, vj, yq);
+                    ys = fma(a, abs(vj), ys);
+                    rs += a;
+                }
+            }
+            q = fma(vi, yq, q);
+            s = fma(abs(vi), ys, s);
+            v2 = fma(vi, vi, v2);
+            rmax = max(rmax, rs);
+            u[h] = (i < n) ? yq : T(0);
+        }
+        q = warp_sum(q);
+        s = warp_sum(s);
+        v2 = warp_sum(v2);
+        if (it == 0) {
+            band = amb * sqrt(warp_sum(f2));
+            anorm = warp_max(rmax);
+        }
+        if (q < -(g * s + band * v2)) return true;
+        if (it == kNotPdSteps) return false;
+        // v <- ||C||_inf v - |C| v, scaled by its largest entry
+        T um = T(0);
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            const int i = lane + 32 * h;
+            u[h] = (i < n) ? fma(anorm, ub[i], -u[h]) : T(0);
+            um = max(um, abs(u[h]));
+        }
+        um = warp_max(um);
+        if (!(um > T(0))) return false;
+        const T ru = T(1) / um;
+        __syncwarp();
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            const int i = lane + 32 * h;
+            if (i < n) ub[i] = u[h] * ru;
+        }
+        __syncwarp();
+    }
+}
+
 // ------------------------------------------------------------------------
 // per-pixel driver
 // ------------------------------------------------------------------------
@@ -1587,13 +1681,24 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
         const T anorm = warp_max(rs);          // |C| inf-norm
         __syncwarp();
         bool ok;
-        if constexpr (sizeof(T) == 4 && NP <= 32)
-            ok = warp_sweep_inverse_rows<LD, NP>(reinterpret_cast<float *>(Xr), nn,
-                                                  reinterpret_cast<float *>(sm + L::wk), &xnorm, lane);
-        else
-            ok = warp_sweep_inverse<T, LD, NP>(Xr, nn, yv, &xnorm, lane);
+        int kfail = 0;
+        const T *rk;
+        if constexpr (sizeof(T) == 4 && NP <= 32) {
+            float *rowb = reinterpret_cast<float *>(sm + L::wk);
+            ok = warp_sweep_inverse_rows<LD, NP>(reinterpret_cast<float *>(Xr), nn, rowb, &xnorm, lane, &kfail);
+            rk = reinterpret_cast<const T *>(rowb + (kfail & 1) * NP);
+        } else {
+            ok = warp_sweep_inverse<T, LD, NP>(Xr, nn, yv, &xnorm, lane, &kfail);
+            rk = yv;
+        }
         if (!fp32) return ok ? 1 : -1;
-        if (!ok) return 0;                     // FP32 pivot failure: settle in FP64
+        if (!ok) {
+            // FP32 pivot failure: |C| clearly not positive definite, or
+            // positive definite but too close to singular for FP32 (settled
+            // in FP64)
+            T *ub = reinterpret_cast<T *>(sm + L::wk) + 3 * NP;     // past the sweep's rows
+            return abs_not_pd<T, NP>(cp, rk, kfail, nn, amb, ub, lane) ? -1 : 0;
+        }
         if (!(anorm * xnorm <= T(P.cond_max))) return 0;
         return 1;
     };
@@ -1628,7 +1733,8 @@ __device__ void pixel_solve(const KParams &P, long long pp, unsigned char *sm, i
             }
         } else {
             if (r < 0) {
-                // FP64: not positive definite, so lambda_min(|C|) <= 0 < 1e-6
+                // not positive definite (FP64, or proved in FP32 by
+                // abs_not_pd), so lambda_min(|C|) <= 0 < 1e-6
                 put_code(P, pp, lane, -4);
                 return;
             }

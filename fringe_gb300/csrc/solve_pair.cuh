@@ -322,14 +322,75 @@ __device__ __forceinline__ C2<float> pair_matvec(const C2<float> *A, int n, cons
     return u;
 }
 
+// |C| not positive definite, proved from a failed sweep: abs_not_pd on the
+// 16 lanes of a half (v = (-w, 1, 0, ..) from row k of the sweep, its
+// quadratic form below minus the rounding and spectral bands, refined by up
+// to kNotPdSteps power steps on ||C||_inf I - |C| when it falls short).
+// Every lane calls it (the rows are read from tensor memory, so the steps
+// run while either half still needs one); go: this half's sweep stopped at
+// step k with row k in rk.  ub: the half's 16 entries of scratch.
+__device__ __forceinline__ bool pair_not_pd(const PairRows &cp, const float *rk, int k, int n, float amb,
+                                            float *ub, const PairHalf &H, bool go)
+{
+    const int i = H.hl;
+    if (go) ub[i] = (i < k) ? -rk[i] : (i == k ? 1.f : 0.f);
+    const float g = float(2 * (n + 1)) * Eps<float>::v;
+    float band = 0.f, anorm = 0.f;
+    bool proved = false, pend = go;
+    for (int it = 0;; ++it) {
+        __syncwarp();
+        const bool row = pend && i < n;
+        const float vi = row ? ub[i] : 0.f;
+        float yq = 0.f, ys = 0.f, rs = 0.f, f2 = 0.f;
+#pragma unroll
+        for (int c = 0; c < PNP / 8; ++c) {
+            C2<float> v[8];
+            cp.load(0, c, v);
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const int j = 8 * c + kk;
+                if (!row || j >= n) continue;
+                const float m2 = cabs2(v[kk]);
+                f2 += m2;
+                const float a = (i == j) ? 1.f : m2 * rsqrtf(max(m2, 1e-37f));
+                const float vj = ub[j];
+                yq = fmaf(a, vj, yq);
+                ys = fmaf(a, fabsf(vj), ys);
+                rs += a;
+            }
+        }
+        const float q = hsum(vi * yq, H.hm);
+        const float sa = hsum(fabsf(vi) * ys, H.hm);
+        const float v2 = hsum(vi * vi, H.hm);
+        if (it == 0) {
+            band = amb * sqrtf(hsum(f2, H.hm));
+            anorm = hmax(rs, H.hm);
+        }
+        if (pend && q < -(g * sa + band * v2)) {
+            proved = true;
+            pend = false;
+        }
+        if (it == kNotPdSteps || !__any_sync(0xffffffffu, pend)) break;
+        // v <- ||C||_inf v - |C| v, scaled by its largest entry
+        const float u = (pend && i < n) ? fmaf(anorm, vi, -yq) : 0.f;
+        const float um = hmax(fabsf(u), H.hm);
+        if (!(um > 0.f)) pend = false;
+        __syncwarp();
+        if (pend && i < n) ub[i] = u * (1.f / um);
+    }
+    __syncwarp();
+    return proved;
+}
+
 // |C| from the coherence rows, its symmetric sweep inverse
 // (warp_sweep_inverse_rows on 16 lanes) and M = inv|C| o C into W
 // (evd.cpp:623-667).  Every lane calls it; go: this half builds M.  Returns
-// true when M is in W: every sweep pivot is > 0, cond_inf(|C|) <= cond_max
-// and 1 / |inv|C||_inf > lim (which settles the lambda_min(|C|) test); false
-// means the pixel goes to the FP64 path.
-__device__ __forceinline__ bool pair_build_M(const PairRows &cp, unsigned char *sm, C2<float> *W, const PairHalf &H,
-                                             bool go, int n, float cond_max, float lim, float *xnorm)
+// 1 when M is in W: every sweep pivot is > 0, cond_inf(|C|) <= cond_max and
+// 1 / |inv|C||_inf > lim (which settles the lambda_min(|C|) test); -1 when a
+// pivot <= 0 proves |C| not positive definite (pair_not_pd); 0 when the
+// pixel goes to the FP64 path.  amb: the rounding band per unit of ||C||_F.
+__device__ __forceinline__ int pair_build_M(const PairRows &cp, unsigned char *sm, C2<float> *W, const PairHalf &H,
+                                            bool go, int n, float cond_max, float lim, float amb, float *xnorm)
 {
     constexpr int LD = PLay::LD;
     const int i = H.hl;
@@ -352,10 +413,11 @@ __device__ __forceinline__ bool pair_build_M(const PairRows &cp, unsigned char *
     }
     const float anorm = hmax(rs, H.hm);
     bool ok = go;
+    int kfail = -1;
+    float *rowb = reinterpret_cast<float *>(sm + PLay::wk);
     if (ok) {
         // lane k publishes row k with its k-th entry replaced by p - 1 (see
         // warp_sweep_inverse_rows)
-        float *rowb = reinterpret_cast<float *>(sm + PLay::wk);
 #pragma unroll 1
         for (int k = 0; k < n; ++k) {
             float *rk = rowb + (k & 1) * PNP;
@@ -371,6 +433,7 @@ __device__ __forceinline__ bool pair_build_M(const PairRows &cp, unsigned char *
             const float p = *pk;
             if (!(p > 0.f)) {
                 ok = false;
+                kfail = k;
                 break;
             }
             const float rp = 1.f / p;
@@ -397,6 +460,10 @@ __device__ __forceinline__ bool pair_build_M(const PairRows &cp, unsigned char *
         *xnorm = hmax(s, H.hm);
         ok = anorm * (*xnorm) <= cond_max && 1.f / *xnorm > lim;
     }
+    const bool failed = kfail >= 0;
+    bool not_pd = false;
+    if (__any_sync(0xffffffffu, failed))
+        not_pd = pair_not_pd(cp, rowb + (kfail & 1) * PNP, kfail, n, amb, rowb + 3 * PNP, H, failed);
     // M = inv|C| o C
     __syncwarp();
 #pragma unroll
@@ -410,7 +477,7 @@ __device__ __forceinline__ bool pair_build_M(const PairRows &cp, unsigned char *
         }
     }
     __syncwarp();
-    return ok;
+    return ok ? 1 : (not_pd ? -1 : 0);
 }
 
 // two power iterations on C from the all-ones vector (warp_power_start);
@@ -564,9 +631,12 @@ __device__ void pair_mle(const KParams &P, long long pp, unsigned char *slab0, c
     // ---- |C|, its inverse and M = inv|C| o C (evd.cpp:623-667) -------------
     const float lim = thr + amb * float(n);
     float xnorm = 0.f;
-    if (!pair_build_M(cp, sm, Wm, H, act, n, P.cond_max, lim, &xnorm) && act) {
-        defer_fp64(P, pp, hl);
-        act = false;
+    {
+        const int r = pair_build_M(cp, sm, Wm, H, act, n, P.cond_max, lim, amb, &xnorm);
+        // not positive definite, so lambda_min(|C|) <= 0 < 1e-6 (evd.cpp:626-641)
+        if (act && r < 0) put_code(P, pp, hl, -4);
+        if (act && r == 0) defer_fp64(P, pp, hl);
+        act = act && r > 0;
     }
     float tr = 0.f, dM = 0.f;
     bool dM_exact = false;
@@ -593,7 +663,7 @@ __device__ void pair_mle(const KParams &P, long long pp, unsigned char *slab0, c
     // M again (the factorisation consumed it) for a second shift or for the
     // Householder path
     bool reb = run && st != 1;
-    if (__any_sync(0xffffffffu, reb)) pair_build_M(cp, sm, Wm, H, reb, n, P.cond_max, lim, &xnorm);
+    if (__any_sync(0xffffffffu, reb)) pair_build_M(cp, sm, Wm, H, reb, n, P.cond_max, lim, amb, &xnorm);
     if (reb) {
         if (hl == 0) atomicAdd(P.slow, 1);
         float sigma1;
@@ -613,7 +683,7 @@ __device__ void pair_mle(const KParams &P, long long pp, unsigned char *slab0, c
             reb = st != 1;
         }
     }
-    if (__any_sync(0xffffffffu, reb)) pair_build_M(cp, sm, Wm, H, reb, n, P.cond_max, lim, &xnorm);
+    if (__any_sync(0xffffffffu, reb)) pair_build_M(cp, sm, Wm, H, reb, n, P.cond_max, lim, amb, &xnorm);
     const bool hh_need = act && st != 1;
     float eig_hi = 0.f;
     if (hh_need) {
