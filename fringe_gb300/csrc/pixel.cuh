@@ -1333,8 +1333,9 @@ __device__ bool abs_not_pd(const CP &cp, const T *rk, int k, int n, T amb, T *ub
 // per-pixel driver
 // ------------------------------------------------------------------------
 // power iterations on C from the all-ones vector that start the MLE
-// inverse iteration
-constexpr int kPowerStartIters = 2;
+// inverse iteration (one: a second cost more solve time than the inverse
+// iteration steps it saved)
+constexpr int kPowerStartIters = 1;
 
 // register block of the upper triangle of Gamma each lane accumulates
 // (BR rows x BC columns): 8 x 4 in FP32 and 4 x 4 in FP64 give 20 and 36

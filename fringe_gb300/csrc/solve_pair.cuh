@@ -480,7 +480,7 @@ __device__ __forceinline__ int pair_build_M(const PairRows &cp, unsigned char *s
     return ok ? 1 : (not_pd ? -1 : 0);
 }
 
-// two power iterations on C from the all-ones vector (warp_power_start);
+// kPowerStartIters power iterations on C from the all-ones vector (warp_power_start);
 // every lane calls it.  The unit vector comes back in z and in vv.
 __device__ __forceinline__ C2<float> pair_power_start(const PairRows &cp, int n, unsigned char *sm,
                                                       const PairHalf &H)
