@@ -146,6 +146,22 @@ def simulate_stack(rows: int, cols: int, nbands: int, seed: int, *,
     return x.reshape(nbands, rows, cols)
 
 
+def indefinite_abs_coherence(nbands: int, rng: np.random.Generator,
+                              below: float = -0.3) -> np.ndarray:
+    """A coherence matrix C0 = V V^H + 0.02 I (V complex, nbands x 2) scaled
+    to a unit diagonal, drawn until its magnitude |C0| has an eigenvalue
+    below `below`.  C0 is positive definite; the sample coherence of a
+    window of its draws keeps an indefinite magnitude (the reference's code
+    -4 in the evd module, the EVD fall-back in phase_link)."""
+    while True:
+        V = rng.standard_normal((nbands, 2)) + 1j * rng.standard_normal((nbands, 2))
+        C0 = V @ V.conj().T + 0.02 * np.eye(nbands)
+        d = np.sqrt(np.real(np.diag(C0)))
+        C0 = C0 / np.outer(d, d)
+        if np.linalg.eigvalsh(np.abs(C0))[0] < below:
+            return C0
+
+
 def scene(kind: str, rows: int, cols: int, nbands: int, ny: int, nx: int,
           seed: int):
     """Build (stack, nmap) for one of the workload families.
@@ -155,10 +171,19 @@ def scene(kind: str, rows: int, cols: int, nbands: int, ny: int, nx: int,
                         nmap = same-class neighbours.
     kind = "illcond"  : gamma0 ~ U(0.05, 0.9) per pixel, 10% of pixels with
                         gamma_inf = 0 (else 0.2), Voronoi nmap.
+    kind = "indefabs" : every pixel drawn from one positive definite
+                        coherence whose magnitude matrix is indefinite (see
+                        indefinite_abs_coherence), nmap all ones.
     """
     rng = np.random.Generator(np.random.PCG64(seed + 7919))
     if kind == "uniform":
         st = simulate_stack(rows, cols, nbands, seed)
+        return st, nmap_all_ones(rows, cols, ny, nx)
+    if kind == "indefabs":
+        L = np.linalg.cholesky(indefinite_abs_coherence(nbands, rng))
+        z = (rng.standard_normal((nbands, rows * cols))
+             + 1j * rng.standard_normal((nbands, rows * cols))) / np.sqrt(2.0)
+        st = (L @ z).reshape(nbands, rows, cols).astype(np.complex64)
         return st, nmap_all_ones(rows, cols, ny, nx)
     classes = voronoi_classes(rows, cols, 8, rng)
     amp = (1.0 + 0.5 * classes).astype(np.float32)

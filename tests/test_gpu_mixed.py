@@ -130,35 +130,19 @@ def test_mixed_out_of_range_samples(gpu_lib, nb):
         assert np.array_equal(g["tcorr"][3:8, 4:11] < 0, o["tcorr"][3:8, 4:11] < 0)
 
 
-def _indefinite_abs_scene(R, C, n, ny, nx, seed):
-    """Every pixel drawn from one coherence C0 = V V^H + 0.02 I (V complex,
-    n x 2, scaled to a unit diagonal).  C0 is positive definite, but its
-    magnitude |C0| has a negative eigenvalue (below -0.3, picked by seed), so
-    the sample coherence over a full window has an indefinite |C|: code -4
-    in the evd semantics, the EVD fall-back in the phase_link semantics."""
-    rng = np.random.default_rng(seed)
-    while True:
-        V = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
-        C0 = V @ V.conj().T + 0.02 * np.eye(n)
-        d = np.sqrt(np.real(np.diag(C0)))
-        C0 = C0 / np.outer(d, d)
-        if np.linalg.eigvalsh(np.abs(C0))[0] < -0.3:
-            break
-    L = np.linalg.cholesky(C0)
-    z = (rng.standard_normal((n, R * C)) + 1j * rng.standard_normal((n, R * C))) / np.sqrt(2)
-    return (L @ z).reshape(n, R, C).astype(np.complex64), synth.nmap_all_ones(R, C, ny, nx)
-
-
 @pytest.mark.parametrize("precision", ["mixed", "fp32"])
 @pytest.mark.parametrize("nb", [6, 24])
 def test_indefinite_abs_coherence_resolved_in_fp32(gpu_lib, precision, nb):
-    """A failed FP32 sweep of |C| whose failing row gives a quadratic form
-    below minus the error bands proves |C| not positive definite, so these
-    pixels get their code (or the EVD fall-back) without the FP64 path.
-    Six dates run the two-pixels-per-warp solve of the mixed form."""
+    """Every pixel of the scene has an indefinite |C| (its C drawn from a
+    positive definite coherence whose magnitude matrix is indefinite).  A
+    failed FP32 sweep of |C| whose failing row, after at most a few power
+    steps, gives a quadratic form below minus the error bands proves |C| not
+    positive definite, so these pixels get their code (or the EVD fall-back)
+    without the FP64 path.  Six dates run the two-pixels-per-warp solve of
+    the mixed form."""
     from fringe_gb300 import _lib, phase_link
     from tests.parity import codes
-    stack, nmap = _indefinite_abs_scene(24, 40, nb, 5, 10, seed=50 + nb)
+    stack, nmap = synth.scene("indefabs", 24, 40, nb, 5, 10, seed=50 + nb)
     ctx = _lib.Context(0)
     for sem in ("evd", "phase_link"):
         g = phase_link(stack, nmap, (5, 10), method="MLE", semantics=sem, precision=precision, ctx=ctx)

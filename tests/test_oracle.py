@@ -124,6 +124,25 @@ def test_row_ranges_are_block_invariant():
         assert np.array_equal(joined, full[k]), k
 
 
+@pytest.mark.parametrize("nb", [6, 24])
+def test_indefinite_abs_scene_codes(nb):
+    """The "indefabs" scene (every pixel drawn from a positive definite
+    coherence whose magnitude matrix is indefinite) is what the GPU test of
+    the FP32 not-positive-definite proof relies on: the evd module reports
+    -4 for every pixel (the Cholesky of |C| fails, src/evd/evd.cpp:626-641),
+    and phase_link falls back to the EVD estimator for every pixel
+    (src/phase_link/phase_link.cpp:540-618), so its MLE output equals its
+    EVD output."""
+    stack, nmap = synth.scene("indefabs", 16, 24, nb, 5, 10, seed=50 + nb)
+    evd = oracle.run(stack, nmap, 5, 10, method="MLE", semantics="evd")
+    assert np.all(evd["tcorr"] == -4)
+    mle = oracle.run(stack, nmap, 5, 10, method="MLE", semantics="phase_link")
+    ref = oracle.run(stack, nmap, 5, 10, method="EVD", semantics="phase_link")
+    assert np.all(mle["tcorr"] > 0)
+    for k in ("phase", "tcorr", "comp"):
+        assert np.array_equal(mle[k], ref[k]), k
+
+
 def test_oracle_rejects_invalid_options():
     stack, nmap = synth.scene("uniform", 8, 8, 6, 1, 1, seed=1)
     with pytest.raises(ValueError):
