@@ -568,6 +568,7 @@ def illcond_measurement(ctx, cpu_rows=24, size=1024):
         for _ in range(2):
             out = phase_link(d, dn, (NY, NX), method="MLE", precision=prec, ctx=ctx, out=out)
         torch.cuda.synchronize()
+        ctx.set_profiling(True)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -576,8 +577,12 @@ def illcond_measurement(ctx, cpu_rows=24, size=1024):
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / 3
+        _, _, runs = ctx.profile()
+        kms = {k: v / max(runs, 1) for k, v in ctx.profile_kernels().items() if v > 0}
+        ctx.set_profiling(False)
         outs[prec] = out
         res[prec] = {"value": size * size / ms * 1e3, "unit": "px/s", "ms": ms,
+                     "kernel_ms": kms,
                      "fp64_settled_px": int(fp64_px), "fp64_settled_share": fp64_px / float(size * size)}
     ref = {k: torch.zeros_like(v) for k, v in outs["mixed"].items()}
     ctx.set_tuning(force_fp64=True)
