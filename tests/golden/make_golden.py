@@ -32,6 +32,9 @@ CASES = {
                    ("MLE", "phase_link", {"min_neighbors": 5}),
                    ("MLE", "evd", {"mini_stack_count": 3})]),
     "illcond64": ("illcond", 12, 16, 64, 5, 10, 1003, [("MLE", "evd", {})]),
+    # |C| indefinite in every pixel: code -4 (evd), the EVD fall-back (phase_link)
+    "indefabs6": ("indefabs", 12, 16, 6, 5, 10, 56, [("MLE", "evd", {}), ("MLE", "phase_link", {})]),
+    "indefabs24": ("indefabs", 12, 16, 24, 5, 10, 74, [("MLE", "evd", {}), ("MLE", "phase_link", {})]),
 }
 
 

@@ -10,7 +10,7 @@ import pytest
 
 import oracle
 from fringe_gb300 import synth
-from tests.parity import assert_parity, compare, load_golden
+from tests.parity import assert_parity, codes, compare, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -215,7 +215,8 @@ def test_golden_vectors_from_the_reference(gpu_lib):
             got = phase_link(g["stack"], g["nmap"], (g["ny"], g["nx"]), method=method,
                              semantics=sem, **extra)
             m = compare(got, ref)
-            assert m["valid_both"] > 0, (case, var, m)
+            # a variant may code every pixel (-4 everywhere on the indefinite-|C| scenes)
+            assert m["valid_both"] > 0 or np.all(codes(ref) < 0), (case, var, m)
             assert_parity(m)
 
 

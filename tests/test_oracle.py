@@ -8,7 +8,7 @@ import pytest
 
 import oracle
 from fringe_gb300 import synth
-from tests.parity import assert_parity, compare, load_golden
+from tests.parity import assert_parity, codes, compare, load_golden
 
 # the known 3x3 matrix of tests/eigen/test_eig.cpp:55-64
 A3 = np.array([[3, -2, 4], [-2, 8, 2], [4, 2, 3]], dtype=np.complex128)
@@ -92,7 +92,8 @@ def test_port_matches_reference_golden_vectors(golden):
             got = oracle.run(g["stack"], g["nmap"], g["ny"], g["nx"], method=method,
                              semantics=sem, **extra)
             m = compare(got, ref)
-            assert m["valid_both"] > 0, (case, var, m)
+            # a variant may code every pixel (-4 everywhere on the indefinite-|C| scenes)
+            assert m["valid_both"] > 0 or np.all(codes(ref) < 0), (case, var, m)
             assert_parity(m, phase_tol=1e-6, tcorr_tol=1e-6)
             assert m["phase_max"] < 1e-5, (case, var, m)
 
