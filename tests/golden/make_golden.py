@@ -32,6 +32,11 @@ CASES = {
                    ("MLE", "phase_link", {"min_neighbors": 5}),
                    ("MLE", "evd", {"mini_stack_count": 3})]),
     "illcond64": ("illcond", 12, 16, 64, 5, 10, 1003, [("MLE", "evd", {})]),
+    # edge depths: one date (tcorr 0/0 = NaN), two, and 17 (padded date pairs; -2 and -4 codes)
+    "depth1": ("voronoi", 12, 16, 1, 2, 3, 101, [("MLE", "evd", {}), ("EVD", "evd", {})]),
+    "depth2": ("voronoi", 12, 16, 2, 2, 3, 102, [("MLE", "evd", {}), ("EVD", "evd", {})]),
+    "depth17": ("voronoi", 12, 16, 17, 2, 3, 117, [("MLE", "evd", {}), ("EVD", "evd", {}),
+                                                   ("MLE", "phase_link", {})]),
     # |C| indefinite in every pixel: code -4 (evd), the EVD fall-back (phase_link)
     "indefabs6": ("indefabs", 12, 16, 6, 5, 10, 56, [("MLE", "evd", {}), ("MLE", "phase_link", {})]),
     "indefabs24": ("indefabs", 12, 16, 24, 5, 10, 74, [("MLE", "evd", {}), ("MLE", "phase_link", {})]),
