@@ -31,7 +31,9 @@ CASES = {
                   [("MLE", "evd", {}), ("EVD", "evd", {}), ("STBAS", "evd", {"band_width": 5}),
                    ("MLE", "phase_link", {"min_neighbors": 5}),
                    ("MLE", "evd", {"mini_stack_count": 3})]),
-    "illcond64": ("illcond", 12, 16, 64, 5, 10, 1003, [("MLE", "evd", {})]),
+    "illcond64": ("illcond", 12, 16, 64, 5, 10, 1003, [("MLE", "evd", {}), ("EVD", "evd", {}),
+                                                       ("STBAS", "evd", {"band_width": 10}),
+                                                       ("MLE", "phase_link", {})]),
     # edge depths: one date (tcorr 0/0 = NaN), two, and 17 (padded date pairs; -2 and -4 codes)
     "depth1": ("voronoi", 12, 16, 1, 2, 3, 101, [("MLE", "evd", {}), ("EVD", "evd", {})]),
     "depth2": ("voronoi", 12, 16, 2, 2, 3, 102, [("MLE", "evd", {}), ("EVD", "evd", {})]),
