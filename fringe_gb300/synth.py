@@ -147,19 +147,23 @@ def simulate_stack(rows: int, cols: int, nbands: int, seed: int, *,
 
 
 def indefinite_abs_coherence(nbands: int, rng: np.random.Generator,
-                              below: float = -0.3) -> np.ndarray:
+                              below: float = -0.3, tries: int = 20000) -> np.ndarray:
     """A coherence matrix C0 = V V^H + 0.02 I (V complex, nbands x 2) scaled
     to a unit diagonal, drawn until its magnitude |C0| has an eigenvalue
     below `below`.  C0 is positive definite; the sample coherence of a
     window of its draws keeps an indefinite magnitude (the reference's code
-    -4 in the evd module, the EVD fall-back in phase_link)."""
-    while True:
+    -4 in the evd module, the EVD fall-back in phase_link).  From 4 dates up
+    a draw is found quickly; at 2 none exists (a 2 x 2 |C0| is positive
+    semi-definite) and at 3 none turned up in 20,000 draws: ValueError after
+    `tries` draws."""
+    for _ in range(tries):
         V = rng.standard_normal((nbands, 2)) + 1j * rng.standard_normal((nbands, 2))
         C0 = V @ V.conj().T + 0.02 * np.eye(nbands)
         d = np.sqrt(np.real(np.diag(C0)))
         C0 = C0 / np.outer(d, d)
         if np.linalg.eigvalsh(np.abs(C0))[0] < below:
             return C0
+    raise ValueError("no %d-date coherence with lambda_min(|C|) < %g in %d draws" % (nbands, below, tries))
 
 
 def scene(kind: str, rows: int, cols: int, nbands: int, ny: int, nx: int,
