@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "fringe_gb300.h"
+#include "guard.h"
 #include "ctx.h"
 #include "kernels.h"
 #include "pixel.cuh"
@@ -128,6 +129,7 @@ const char *fpl_error_string(int code)
     case FPL_ERR_DEVICE_CHECK: return "a kernel reported an internal error";
     case FPL_ERR_NULL: return "a required pointer is NULL";
     case FPL_ERR_TIMEOUT: return "timed out waiting for a served job";
+    case FPL_ERR_HOST: return "host-side failure (out of host memory, or no thread could be started)";
     case FPL_ERR_NOALLOC_LIMIT: return "job exceeds the FPL_NOALLOC_MAX_PIXELS scratch of fpl_run_noalloc";
     }
     return "unknown error";
@@ -135,55 +137,61 @@ const char *fpl_error_string(int code)
 
 int fpl_ctx_create(int device, fpl_ctx **out)
 {
-    if (!out) return FPL_ERR_NULL;
-    *out = nullptr;
-    int ndev = 0;
-    cudaError_t e = cudaGetDeviceCount(&ndev);
-    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
-    if (device < 0 || device >= ndev) return FPL_ERR_OPTIONS;
-    e = cudaSetDevice(device);
-    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
-    fpl_ctx *ctx = new fpl_ctx();
-    ctx->device = device;
-    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
-    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { delete ctx; return cuda_fail(nullptr, e, "cudaStreamCreate"); }
-    cudaEventCreate(&ctx->ev0);
-    cudaEventCreate(&ctx->ev1);
-    cudaEventCreateWithFlags(&ctx->ev_last, cudaEventDisableTiming);
-    e = cudaMalloc(&ctx->d_small, kCounterBlock * kRunChunks);
-    if (e != cudaSuccess) { fpl_ctx_destroy(ctx); return cuda_fail(nullptr, e, "cudaMalloc"); }
-    *out = ctx;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!out) return FPL_ERR_NULL;
+        *out = nullptr;
+        int ndev = 0;
+        cudaError_t e = cudaGetDeviceCount(&ndev);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
+        if (device < 0 || device >= ndev) return FPL_ERR_OPTIONS;
+        e = cudaSetDevice(device);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+        fpl_ctx *ctx = new fpl_ctx();
+        ctx->device = device;
+        cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+        e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete ctx; return cuda_fail(nullptr, e, "cudaStreamCreate"); }
+        cudaEventCreate(&ctx->ev0);
+        cudaEventCreate(&ctx->ev1);
+        cudaEventCreateWithFlags(&ctx->ev_last, cudaEventDisableTiming);
+        e = cudaMalloc(&ctx->d_small, kCounterBlock * kRunChunks);
+        if (e != cudaSuccess) { fpl_ctx_destroy(ctx); return cuda_fail(nullptr, e, "cudaMalloc"); }
+        *out = ctx;
+        return FPL_OK;
+    });
 }
 
 int fpl_ctx_destroy(fpl_ctx *ctx)
 {
-    if (!ctx) return FPL_OK;
-    cudaSetDevice(ctx->device);
-    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
-    for (cudaEvent_t e : ctx->chunk_ev) cudaEventDestroy(e);
-    if (ctx->s_in) cudaStreamDestroy(ctx->s_in);
-    if (ctx->s_out) cudaStreamDestroy(ctx->s_out);
-    void *bufs[] = {ctx->d_stack, ctx->d_nmap, ctx->d_phase, ctx->d_tcorr, ctx->d_comp,
-                    ctx->d_status, ctx->d_fb_list, ctx->d_small, ctx->d_cbuf, ctx->d_cinfo,
-                    ctx->d_nm, ctx->d_pack};
-    for (void *b : bufs)
-        if (b) cudaFree(b);
-    if (ctx->ev_last) cudaEventDestroy(ctx->ev_last);
-    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
-    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx) return FPL_OK;
+        cudaSetDevice(ctx->device);
+        if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+        for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+        for (cudaEvent_t e : ctx->chunk_ev) cudaEventDestroy(e);
+        if (ctx->s_in) cudaStreamDestroy(ctx->s_in);
+        if (ctx->s_out) cudaStreamDestroy(ctx->s_out);
+        void *bufs[] = {ctx->d_stack, ctx->d_nmap, ctx->d_phase, ctx->d_tcorr, ctx->d_comp,
+                        ctx->d_status, ctx->d_fb_list, ctx->d_small, ctx->d_cbuf, ctx->d_cinfo,
+                        ctx->d_nm, ctx->d_pack};
+        for (void *b : bufs)
+            if (b) cudaFree(b);
+        if (ctx->ev_last) cudaEventDestroy(ctx->ev_last);
+        if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+        if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return FPL_OK;
+    });
 }
 
 int fpl_last_stats(const fpl_ctx *ctx, fpl_stats *out)
 {
-    if (!ctx || !out) return FPL_ERR_NULL;
-    *out = ctx->stats;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx || !out) return FPL_ERR_NULL;
+        *out = ctx->stats;
+        return FPL_OK;
+    });
 }
 
 }  // extern "C"
@@ -350,29 +358,33 @@ extern "C" {
 int fpl_adjust_wrapped(fpl_ctx *ctx, const void *phase, const void *datum, void *out,
                        int ndates, long long npix, void *stream)
 {
-    if (!ctx || !phase || !datum || !out) return FPL_ERR_NULL;
-    if (ndates < 0 || npix < 0) return FPL_ERR_OPTIONS;
-    if (ndates == 0 || npix == 0) return FPL_OK;
-    FPL_CUDA(ctx, cudaSetDevice(ctx->device));
-    long long blocks = std::min<long long>((npix + 255) / 256, (long long)ctx->num_sms * 8);
-    k_adjust_wrapped<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const float2 *>(phase), static_cast<const float2 *>(datum),
-        static_cast<float2 *>(out), ndates, npix);
-    FPL_CUDA(ctx, cudaGetLastError());
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx || !phase || !datum || !out) return FPL_ERR_NULL;
+        if (ndates < 0 || npix < 0) return FPL_ERR_OPTIONS;
+        if (ndates == 0 || npix == 0) return FPL_OK;
+        FPL_CUDA(ctx, cudaSetDevice(ctx->device));
+        long long blocks = std::min<long long>((npix + 255) / 256, (long long)ctx->num_sms * 8);
+        k_adjust_wrapped<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const float2 *>(phase), static_cast<const float2 *>(datum),
+            static_cast<float2 *>(out), ndates, npix);
+        FPL_CUDA(ctx, cudaGetLastError());
+        return FPL_OK;
+    });
 }
 
 int fpl_run_async(fpl_ctx *ctx, const fpl_job *job, void *stream)
 {
-    if (!ctx) return FPL_ERR_NULL;
-    int rc = fpl_validate_job(job);
-    if (rc) return rc;
-    if (job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
-    FPL_CUDA(ctx, cudaSetDevice(ctx->device));
-    // the stream is used as given: NULL is the legacy default stream
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    return fpl_enqueue(ctx, job, job->stack, job->nmap, job->phase, job->tcorr, job->comp,
-                       job->status, st, ctx->force_fp64, ctx->d_small, true);
+    return fpl_guard([&]() -> int {
+        if (!ctx) return FPL_ERR_NULL;
+        int rc = fpl_validate_job(job);
+        if (rc) return rc;
+        if (job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
+        FPL_CUDA(ctx, cudaSetDevice(ctx->device));
+        // the stream is used as given: NULL is the legacy default stream
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        return fpl_enqueue(ctx, job, job->stack, job->nmap, job->phase, job->tcorr, job->comp,
+                           job->status, st, ctx->force_fp64, ctx->d_small, true);
+    });
 }
 
 // host threads that put the FP64-settled pixels in place after a host-memory run
@@ -386,254 +398,273 @@ constexpr int kScatterThreads = 8;
 // its own block of counters so the statistics add up over the run.
 int fpl_run(fpl_ctx *ctx, const fpl_job *job)
 {
-    if (!ctx) return FPL_ERR_NULL;
-    int rc = fpl_validate_job(job);
-    if (rc) return rc;
-    auto t0 = std::chrono::steady_clock::now();
-    FPL_CUDA(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t st = ctx->stream;
-    const int rows = job->rows, cols = job->cols, nb = job->nbands, ny = job->half_window_y;
-    const size_t plane = (size_t)rows * cols;
-    const int nulong = ((2 * job->half_window_y + 1) * (2 * job->half_window_x + 1) + 31) / 32;
-    const size_t b_stack = plane * nb * 8, b_nmap = plane * nulong * 4;
-    const size_t b_tc = plane * 4, b_comp = plane * 8, b_st = plane * 4;
-    const int r0 = job->row_begin, r1 = job->row_end <= 0 ? rows : job->row_end;
-    int nchunks = 1;
-    if (job->memory == FPL_MEM_DEVICE) {
-        FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
-        rc = fpl_enqueue(ctx, job, job->stack, job->nmap, job->phase, job->tcorr, job->comp, job->status, st,
-                         ctx->force_fp64, ctx->d_small, true);
+    return fpl_guard([&]() -> int {
+        if (!ctx) return FPL_ERR_NULL;
+        int rc = fpl_validate_job(job);
         if (rc) return rc;
-        FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
-    } else {
-        if ((rc = grow(ctx, &ctx->d_stack, &ctx->cap_stack, b_stack))) return rc;
-        if ((rc = grow(ctx, &ctx->d_nmap, &ctx->cap_nmap, b_nmap))) return rc;
-        if ((rc = grow(ctx, &ctx->d_phase, &ctx->cap_phase, b_stack))) return rc;
-        if ((rc = grow(ctx, &ctx->d_tcorr, &ctx->cap_tcorr, b_tc))) return rc;
-        if ((rc = grow(ctx, &ctx->d_comp, &ctx->cap_comp, b_comp))) return rc;
-        if (job->status && (rc = grow(ctx, &ctx->d_status, &ctx->cap_status, b_st))) return rc;
-        if (!ctx->s_in) FPL_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_in, cudaStreamNonBlocking));
-        if (!ctx->s_out) FPL_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking));
-        while (ctx->chunk_ev.size() < 2 * (size_t)kRunChunks) {
-            cudaEvent_t e;
-            FPL_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-            ctx->chunk_ev.push_back(e);
-        }
-        char *d_stack = static_cast<char *>(ctx->d_stack);
-        char *d_phase = static_cast<char *>(ctx->d_phase);
-        char *d_comp = static_cast<char *>(ctx->d_comp);
-        uint32_t *d_nmap = static_cast<uint32_t *>(ctx->d_nmap);
-        float *d_tcorr = static_cast<float *>(ctx->d_tcorr);
-        int32_t *d_status = job->status ? static_cast<int32_t *>(ctx->d_status) : nullptr;
-        const char *h_stack = static_cast<const char *>(job->stack);
-        // chunk c computes rows [cb[c], cb[c+1]).  The first chunk's upload
-        // and the last chunk's download overlap no compute, so those chunks
-        // are the smallest (row shares 1,2,3,..,3,2,1, multiples of 8
-        // rows); short ranges are cut into equal chunks of >= 8 rows.
-        int cb[kRunChunks + 1];
-        {
-            static_assert(kRunChunks == 8, "chunk weights");
-            const int wsum[kRunChunks + 1] = {0, 1, 3, 6, 9, 12, 15, 17, 18};
-            const int span = r1 - r0;
-            cb[0] = r0;
-            nchunks = 0;
-            if (span >= 8 * 18) {
-                for (int c = 1; c <= kRunChunks; ++c)
-                    cb[c] = (c == kRunChunks) ? r1 : r0 + (int)((long long)span * wsum[c] / 18) / 8 * 8;
-                nchunks = kRunChunks;
-            } else {
-                int step = (span + kRunChunks - 1) / kRunChunks;
-                step = std::max(8, (step + 7) & ~7);
-                for (int a = r0; a < r1; a += step) cb[++nchunks] = std::min(r1, a + step);
-            }
-            nchunks = std::max(nchunks, 1);
-            if (span <= 0) cb[1] = r1;
-        }
-        int copied = std::max(0, r0 / 8 * 8 - ny);     // first stack row on the device
-        // One work list for the whole run: the chunks append to it and its
-        // FP64 settle runs once, after the last chunk (a settle per chunk
-        // costs a round of the slow FP64 pixels each time); the settled
-        // pixels' outputs then come back packed and are put in place here.
-        const long long run_px = (long long)(r1 - r0) * cols;
-        FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
-        bool first = true;                  // the first chunk clears the counters (starts the list)
-        for (int c = 0; c < nchunks; ++c) {
-            const int a = cb[c], b = cb[c + 1];
-            if (b <= a) continue;
-            // stack rows every computed pixel's window (and the chunk's tiles) read
-            const int need = std::min(rows, (b + 7) / 8 * 8 + ny);
-            if (need > copied) {
-                const size_t off = (size_t)copied * cols * 8;
-                FPL_CUDA(ctx, cudaMemcpy2DAsync(d_stack + off, plane * 8, h_stack + off, plane * 8,
-                                                (size_t)(need - copied) * cols * 8, nb, cudaMemcpyHostToDevice,
-                                                ctx->s_in));
-                copied = need;
-            }
-            FPL_CUDA(ctx, cudaMemcpyAsync(d_nmap + (size_t)a * cols * nulong, job->nmap + (size_t)a * cols * nulong,
-                                          (size_t)(b - a) * cols * nulong * 4, cudaMemcpyHostToDevice, ctx->s_in));
-            cudaEvent_t ev_in = ctx->chunk_ev[2 * c], ev_done = ctx->chunk_ev[2 * c + 1];
-            FPL_CUDA(ctx, cudaEventRecord(ev_in, ctx->s_in));
-            FPL_CUDA(ctx, cudaStreamWaitEvent(st, ev_in, 0));
-            fpl_job cj = *job;
-            cj.row_begin = a;
-            cj.row_end = b;
-            rc = fpl_enqueue(ctx, &cj, d_stack, d_nmap, d_phase, d_tcorr, d_comp, d_status, st, ctx->force_fp64,
-                             ctx->d_small, first, ENQ_KERNELS | (first ? ENQ_RESET : 0), run_px);
+        auto t0 = std::chrono::steady_clock::now();
+        FPL_CUDA(ctx, cudaSetDevice(ctx->device));
+        cudaStream_t st = ctx->stream;
+        const int rows = job->rows, cols = job->cols, nb = job->nbands, ny = job->half_window_y;
+        const size_t plane = (size_t)rows * cols;
+        const int nulong = ((2 * job->half_window_y + 1) * (2 * job->half_window_x + 1) + 31) / 32;
+        const size_t b_stack = plane * nb * 8, b_nmap = plane * nulong * 4;
+        const size_t b_tc = plane * 4, b_comp = plane * 8, b_st = plane * 4;
+        const int r0 = job->row_begin, r1 = job->row_end <= 0 ? rows : job->row_end;
+        int nchunks = 1;
+        if (job->memory == FPL_MEM_DEVICE) {
+            FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+            rc = fpl_enqueue(ctx, job, job->stack, job->nmap, job->phase, job->tcorr, job->comp, job->status, st,
+                             ctx->force_fp64, ctx->d_small, true);
             if (rc) return rc;
-            first = false;
-            FPL_CUDA(ctx, cudaEventRecord(ev_done, st));
-            FPL_CUDA(ctx, cudaStreamWaitEvent(ctx->s_out, ev_done, 0));
-            const size_t off = (size_t)a * cols, cnt = (size_t)(b - a) * cols;
-            FPL_CUDA(ctx, cudaMemcpy2DAsync(static_cast<char *>(job->phase) + off * 8, plane * 8, d_phase + off * 8,
-                                            plane * 8, cnt * 8, nb, cudaMemcpyDeviceToHost, ctx->s_out));
-            FPL_CUDA(ctx, cudaMemcpyAsync(job->tcorr + off, d_tcorr + off, cnt * 4, cudaMemcpyDeviceToHost,
-                                          ctx->s_out));
-            FPL_CUDA(ctx, cudaMemcpyAsync(static_cast<char *>(job->comp) + off * 8, d_comp + off * 8, cnt * 8,
-                                          cudaMemcpyDeviceToHost, ctx->s_out));
-            if (job->status)
-                FPL_CUDA(ctx, cudaMemcpyAsync(job->status + off, d_status + off, cnt * 4, cudaMemcpyDeviceToHost,
-                                              ctx->s_out));
-        }
-        // the FP64 settle of every chunk's list, on the whole range (an empty
-        // range only clears the counters)
-        rc = fpl_enqueue(ctx, job, d_stack, d_nmap, d_phase, d_tcorr, d_comp, d_status, st, ctx->force_fp64,
-                         ctx->d_small, false, first ? ENQ_RESET : ENQ_SETTLE, run_px);
-        if (rc) return rc;
-        FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
-        int head[16];
-        FPL_CUDA(ctx, cudaMemcpyAsync(head, ctx->d_small, kCounterBlock, cudaMemcpyDeviceToHost, st));
-        FPL_CUDA(ctx, cudaStreamSynchronize(st));
-        const long long nset = std::min<long long>(head[0], run_px);
-        if (nset > 0 && !ctx->force_fp64) {
-            const size_t slots = (size_t)nset * (nb + 3);
-            if ((rc = grow(ctx, &ctx->d_pack, &ctx->cap_pack, slots * sizeof(float2)))) return rc;
-            const unsigned blocks = (unsigned)std::min<size_t>((slots + 255) / 256, (size_t)ctx->num_sms * 8);
-            k_pack_settled<<<blocks, 256, 0, st>>>(static_cast<const long long *>(ctx->d_fb_list),
-                                                   static_cast<const int *>(ctx->d_small), (int)nset,
-                                                   reinterpret_cast<const float2 *>(d_phase), d_tcorr,
-                                                   reinterpret_cast<const float2 *>(d_comp), d_status, (long long)plane,
-                                                   nb, static_cast<float2 *>(ctx->d_pack));
-            FPL_CUDA(ctx, cudaGetLastError());
-            ctx->h_pack.resize(slots);
-            FPL_CUDA(ctx, cudaMemcpyAsync(ctx->h_pack.data(), ctx->d_pack, slots * sizeof(float2),
-                                          cudaMemcpyDeviceToHost, st));
-            FPL_CUDA(ctx, cudaStreamSynchronize(st));
-        }
-        // every chunk's outputs are on the host before the settled pixels
-        // are put in place over them
-        FPL_CUDA(ctx, cudaStreamSynchronize(ctx->s_out));
-        if (nset > 0 && !ctx->force_fp64) {
-            // each settled pixel writes one value into each of nb planes far
-            // apart, so the loop waits on cache misses: split it over host
-            // threads (pixels appear once in the list, so the ranges write
-            // disjoint places)
-            float2 *h_phase = static_cast<float2 *>(job->phase), *h_comp = static_cast<float2 *>(job->comp);
-            const float2 *pack = ctx->h_pack.data();
-            auto put = [&](long long e0, long long e1) {
-                for (long long e = e0; e < e1; ++e) {
-                    const float2 *v = pack + (size_t)e * (nb + 3);
-                    uint32_t lo, hi;
-                    int32_t stv;
-                    std::memcpy(&lo, &v[nb + 2].x, 4);
-                    std::memcpy(&hi, &v[nb + 2].y, 4);
-                    std::memcpy(&stv, &v[nb + 1].y, 4);
-                    const long long pp = (long long)(((uint64_t)hi << 32) | lo);
-                    for (int b = 0; b < nb; ++b) h_phase[(size_t)b * plane + pp] = v[b];
-                    h_comp[pp] = v[nb];
-                    job->tcorr[pp] = v[nb + 1].x;
-                    if (job->status) job->status[pp] = stv;
+            FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+        } else {
+            if ((rc = grow(ctx, &ctx->d_stack, &ctx->cap_stack, b_stack))) return rc;
+            if ((rc = grow(ctx, &ctx->d_nmap, &ctx->cap_nmap, b_nmap))) return rc;
+            if ((rc = grow(ctx, &ctx->d_phase, &ctx->cap_phase, b_stack))) return rc;
+            if ((rc = grow(ctx, &ctx->d_tcorr, &ctx->cap_tcorr, b_tc))) return rc;
+            if ((rc = grow(ctx, &ctx->d_comp, &ctx->cap_comp, b_comp))) return rc;
+            if (job->status && (rc = grow(ctx, &ctx->d_status, &ctx->cap_status, b_st))) return rc;
+            if (!ctx->s_in) FPL_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_in, cudaStreamNonBlocking));
+            if (!ctx->s_out) FPL_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking));
+            while (ctx->chunk_ev.size() < 2 * (size_t)kRunChunks) {
+                cudaEvent_t e;
+                FPL_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                ctx->chunk_ev.push_back(e);
+            }
+            char *d_stack = static_cast<char *>(ctx->d_stack);
+            char *d_phase = static_cast<char *>(ctx->d_phase);
+            char *d_comp = static_cast<char *>(ctx->d_comp);
+            uint32_t *d_nmap = static_cast<uint32_t *>(ctx->d_nmap);
+            float *d_tcorr = static_cast<float *>(ctx->d_tcorr);
+            int32_t *d_status = job->status ? static_cast<int32_t *>(ctx->d_status) : nullptr;
+            const char *h_stack = static_cast<const char *>(job->stack);
+            // chunk c computes rows [cb[c], cb[c+1]).  The first chunk's upload
+            // and the last chunk's download overlap no compute, so those chunks
+            // are the smallest (row shares 1,2,3,..,3,2,1, multiples of 8
+            // rows); short ranges are cut into equal chunks of >= 8 rows.
+            int cb[kRunChunks + 1];
+            {
+                static_assert(kRunChunks == 8, "chunk weights");
+                const int wsum[kRunChunks + 1] = {0, 1, 3, 6, 9, 12, 15, 17, 18};
+                const int span = r1 - r0;
+                cb[0] = r0;
+                nchunks = 0;
+                if (span >= 8 * 18) {
+                    for (int c = 1; c <= kRunChunks; ++c)
+                        cb[c] = (c == kRunChunks) ? r1 : r0 + (int)((long long)span * wsum[c] / 18) / 8 * 8;
+                    nchunks = kRunChunks;
+                } else {
+                    int step = (span + kRunChunks - 1) / kRunChunks;
+                    step = std::max(8, (step + 7) & ~7);
+                    for (int a = r0; a < r1; a += step) cb[++nchunks] = std::min(r1, a + step);
                 }
-            };
-            const long long per_thread = 512;
-            const int nt = (int)std::max<long long>(
-                1, std::min<long long>({(long long)kScatterThreads, (long long)std::thread::hardware_concurrency(),
-                                        (nset + per_thread - 1) / per_thread}));
-            if (nt <= 1) {
-                put(0, nset);
-            } else {
-                std::vector<std::thread> pool;
-                const long long step = (nset + nt - 1) / nt;
-                for (int t = 1; t < nt; ++t)
-                    pool.emplace_back(put, std::min(nset, t * step), std::min(nset, (t + 1) * step));
-                put(0, std::min(nset, step));
-                for (std::thread &th : pool) th.join();
+                nchunks = std::max(nchunks, 1);
+                if (span <= 0) cb[1] = r1;
+            }
+            int copied = std::max(0, r0 / 8 * 8 - ny);     // first stack row on the device
+            // One work list for the whole run: the chunks append to it and its
+            // FP64 settle runs once, after the last chunk (a settle per chunk
+            // costs a round of the slow FP64 pixels each time); the settled
+            // pixels' outputs then come back packed and are put in place here.
+            const long long run_px = (long long)(r1 - r0) * cols;
+            FPL_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+            bool first = true;                  // the first chunk clears the counters (starts the list)
+            for (int c = 0; c < nchunks; ++c) {
+                const int a = cb[c], b = cb[c + 1];
+                if (b <= a) continue;
+                // stack rows every computed pixel's window (and the chunk's tiles) read
+                const int need = std::min(rows, (b + 7) / 8 * 8 + ny);
+                if (need > copied) {
+                    const size_t off = (size_t)copied * cols * 8;
+                    FPL_CUDA(ctx, cudaMemcpy2DAsync(d_stack + off, plane * 8, h_stack + off, plane * 8,
+                                                    (size_t)(need - copied) * cols * 8, nb, cudaMemcpyHostToDevice,
+                                                    ctx->s_in));
+                    copied = need;
+                }
+                FPL_CUDA(ctx, cudaMemcpyAsync(d_nmap + (size_t)a * cols * nulong, job->nmap + (size_t)a * cols * nulong,
+                                              (size_t)(b - a) * cols * nulong * 4, cudaMemcpyHostToDevice, ctx->s_in));
+                cudaEvent_t ev_in = ctx->chunk_ev[2 * c], ev_done = ctx->chunk_ev[2 * c + 1];
+                FPL_CUDA(ctx, cudaEventRecord(ev_in, ctx->s_in));
+                FPL_CUDA(ctx, cudaStreamWaitEvent(st, ev_in, 0));
+                fpl_job cj = *job;
+                cj.row_begin = a;
+                cj.row_end = b;
+                rc = fpl_enqueue(ctx, &cj, d_stack, d_nmap, d_phase, d_tcorr, d_comp, d_status, st, ctx->force_fp64,
+                                 ctx->d_small, first, ENQ_KERNELS | (first ? ENQ_RESET : 0), run_px);
+                if (rc) return rc;
+                first = false;
+                FPL_CUDA(ctx, cudaEventRecord(ev_done, st));
+                FPL_CUDA(ctx, cudaStreamWaitEvent(ctx->s_out, ev_done, 0));
+                const size_t off = (size_t)a * cols, cnt = (size_t)(b - a) * cols;
+                FPL_CUDA(ctx, cudaMemcpy2DAsync(static_cast<char *>(job->phase) + off * 8, plane * 8, d_phase + off * 8,
+                                                plane * 8, cnt * 8, nb, cudaMemcpyDeviceToHost, ctx->s_out));
+                FPL_CUDA(ctx, cudaMemcpyAsync(job->tcorr + off, d_tcorr + off, cnt * 4, cudaMemcpyDeviceToHost,
+                                              ctx->s_out));
+                FPL_CUDA(ctx, cudaMemcpyAsync(static_cast<char *>(job->comp) + off * 8, d_comp + off * 8, cnt * 8,
+                                              cudaMemcpyDeviceToHost, ctx->s_out));
+                if (job->status)
+                    FPL_CUDA(ctx, cudaMemcpyAsync(job->status + off, d_status + off, cnt * 4, cudaMemcpyDeviceToHost,
+                                                  ctx->s_out));
+            }
+            // the FP64 settle of every chunk's list, on the whole range (an empty
+            // range only clears the counters)
+            rc = fpl_enqueue(ctx, job, d_stack, d_nmap, d_phase, d_tcorr, d_comp, d_status, st, ctx->force_fp64,
+                             ctx->d_small, false, first ? ENQ_RESET : ENQ_SETTLE, run_px);
+            if (rc) return rc;
+            FPL_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+            int head[16];
+            FPL_CUDA(ctx, cudaMemcpyAsync(head, ctx->d_small, kCounterBlock, cudaMemcpyDeviceToHost, st));
+            FPL_CUDA(ctx, cudaStreamSynchronize(st));
+            const long long nset = std::min<long long>(head[0], run_px);
+            if (nset > 0 && !ctx->force_fp64) {
+                const size_t slots = (size_t)nset * (nb + 3);
+                if ((rc = grow(ctx, &ctx->d_pack, &ctx->cap_pack, slots * sizeof(float2)))) return rc;
+                const unsigned blocks = (unsigned)std::min<size_t>((slots + 255) / 256, (size_t)ctx->num_sms * 8);
+                k_pack_settled<<<blocks, 256, 0, st>>>(static_cast<const long long *>(ctx->d_fb_list),
+                                                       static_cast<const int *>(ctx->d_small), (int)nset,
+                                                       reinterpret_cast<const float2 *>(d_phase), d_tcorr,
+                                                       reinterpret_cast<const float2 *>(d_comp), d_status, (long long)plane,
+                                                       nb, static_cast<float2 *>(ctx->d_pack));
+                FPL_CUDA(ctx, cudaGetLastError());
+                ctx->h_pack.resize(slots);
+                FPL_CUDA(ctx, cudaMemcpyAsync(ctx->h_pack.data(), ctx->d_pack, slots * sizeof(float2),
+                                              cudaMemcpyDeviceToHost, st));
+                FPL_CUDA(ctx, cudaStreamSynchronize(st));
+            }
+            // every chunk's outputs are on the host before the settled pixels
+            // are put in place over them
+            FPL_CUDA(ctx, cudaStreamSynchronize(ctx->s_out));
+            if (nset > 0 && !ctx->force_fp64) {
+                // each settled pixel writes one value into each of nb planes far
+                // apart, so the loop waits on cache misses: split it over host
+                // threads (pixels appear once in the list, so the ranges write
+                // disjoint places)
+                float2 *h_phase = static_cast<float2 *>(job->phase), *h_comp = static_cast<float2 *>(job->comp);
+                const float2 *pack = ctx->h_pack.data();
+                auto put = [&](long long e0, long long e1) {
+                    for (long long e = e0; e < e1; ++e) {
+                        const float2 *v = pack + (size_t)e * (nb + 3);
+                        uint32_t lo, hi;
+                        int32_t stv;
+                        std::memcpy(&lo, &v[nb + 2].x, 4);
+                        std::memcpy(&hi, &v[nb + 2].y, 4);
+                        std::memcpy(&stv, &v[nb + 1].y, 4);
+                        const long long pp = (long long)(((uint64_t)hi << 32) | lo);
+                        for (int b = 0; b < nb; ++b) h_phase[(size_t)b * plane + pp] = v[b];
+                        h_comp[pp] = v[nb];
+                        job->tcorr[pp] = v[nb + 1].x;
+                        if (job->status) job->status[pp] = stv;
+                    }
+                };
+                const long long per_thread = 512;
+                const int nt = (int)std::max<long long>(
+                    1, std::min<long long>({(long long)kScatterThreads, (long long)std::thread::hardware_concurrency(),
+                                            (nset + per_thread - 1) / per_thread}));
+                if (nt <= 1) {
+                    put(0, nset);
+                } else {
+                    std::vector<std::thread> pool;
+                    pool.reserve(nt - 1);           // only starting a thread can throw below
+                    const long long step = (nset + nt - 1) / nt;
+                    for (int t = 1; t < nt; ++t) {
+                        const long long e0 = std::min(nset, t * step), e1 = std::min(nset, (t + 1) * step);
+                        try {
+                            pool.emplace_back(put, e0, e1);
+                        } catch (...) {
+                            put(e0, e1);            // no thread: this one takes the range
+                        }
+                    }
+                    put(0, std::min(nset, step));
+                    for (std::thread &th : pool) th.join();
+                }
             }
         }
-    }
-    int small[16];
-    FPL_CUDA(ctx, cudaMemcpyAsync(small, ctx->d_small, kCounterBlock, cudaMemcpyDeviceToHost, st));
-    FPL_CUDA(ctx, cudaStreamSynchronize(st));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    const long long fp64 = small[0], slow = small[8];
-    const unsigned err = static_cast<unsigned>(small[4]);
-    ctx->stats.pixels = (long long)(r1 - r0) * cols;
-    ctx->stats.fp64_pixels = ctx->force_fp64 ? ctx->stats.pixels : fp64;
-    ctx->stats.mixed_fp64_inverse = 0;
-    ctx->stats.slow_path_pixels = slow;
-    ctx->stats.kernel_ms = ms;
-    ctx->stats.total_ms =
-        std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (err) {
-        ctx->last_error = "device error flags " + std::to_string(err);
-        return FPL_ERR_DEVICE_CHECK;
-    }
-    return FPL_OK;
+        int small[16];
+        FPL_CUDA(ctx, cudaMemcpyAsync(small, ctx->d_small, kCounterBlock, cudaMemcpyDeviceToHost, st));
+        FPL_CUDA(ctx, cudaStreamSynchronize(st));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        const long long fp64 = small[0], slow = small[8];
+        const unsigned err = static_cast<unsigned>(small[4]);
+        ctx->stats.pixels = (long long)(r1 - r0) * cols;
+        ctx->stats.fp64_pixels = ctx->force_fp64 ? ctx->stats.pixels : fp64;
+        ctx->stats.mixed_fp64_inverse = 0;
+        ctx->stats.slow_path_pixels = slow;
+        ctx->stats.kernel_ms = ms;
+        ctx->stats.total_ms =
+            std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (err) {
+            ctx->last_error = "device error flags " + std::to_string(err);
+            return FPL_ERR_DEVICE_CHECK;
+        }
+        return FPL_OK;
+    });
 }
 
 // test hooks: width of the FP32 ambiguity band, and FP64 for every pixel
 int fpl_ctx_set_tuning(fpl_ctx *ctx, float amb_scale, int force_fp64)
 {
-    if (!ctx) return FPL_ERR_NULL;
-    if (amb_scale >= 0.f) ctx->amb_scale = amb_scale;
-    ctx->force_fp64 = force_fp64 != 0;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx) return FPL_ERR_NULL;
+        if (amb_scale >= 0.f) ctx->amb_scale = amb_scale;
+        ctx->force_fp64 = force_fp64 != 0;
+        return FPL_OK;
+    });
 }
 
 int fpl_ctx_set_shift(fpl_ctx *ctx, float shift, float backoff)
 {
-    if (!ctx) return FPL_ERR_NULL;
-    if (!(shift > 0.f) || !(backoff > 0.f)) return FPL_ERR_OPTIONS;
-    ctx->shift = shift;
-    ctx->shift_backoff = backoff;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx) return FPL_ERR_NULL;
+        if (!(shift > 0.f) || !(backoff > 0.f)) return FPL_ERR_OPTIONS;
+        ctx->shift = shift;
+        ctx->shift_backoff = backoff;
+        return FPL_OK;
+    });
 }
 
 const char *fpl_ctx_last_error(const fpl_ctx *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
 
 int fpl_ctx_set_profiling(fpl_ctx *ctx, int on)
 {
-    if (!ctx) return FPL_ERR_NULL;
-    ctx->profile = on != 0;
-    ctx->prof_tag.clear();
-    ctx->prof_runs = 0;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx) return FPL_ERR_NULL;
+        ctx->profile = on != 0;
+        ctx->prof_tag.clear();
+        ctx->prof_runs = 0;
+        return FPL_OK;
+    });
 }
 
 int fpl_ctx_profile(fpl_ctx *ctx, double *fp32_ms, double *fp64_ms, int *runs)
 {
-    if (!ctx) return FPL_ERR_NULL;
-    double ms[FPL_KTAG_COUNT] = {};
-    for (size_t p = 0; p < ctx->prof_tag.size(); ++p) {
-        FPL_CUDA(ctx, cudaEventSynchronize(ctx->prof_ev[2 * p + 1]));
-        float x = 0.f;
-        FPL_CUDA(ctx, cudaEventElapsedTime(&x, ctx->prof_ev[2 * p], ctx->prof_ev[2 * p + 1]));
-        ms[ctx->prof_tag[p]] += x;
-    }
-    for (int t = 0; t < FPL_KTAG_COUNT; ++t) ctx->prof_ms[t] = ms[t];
-    if (fp32_ms) *fp32_ms = ms[FPL_KTAG_FP32] + ms[FPL_KTAG_GRAM] + ms[FPL_KTAG_SOLVE];
-    if (fp64_ms) *fp64_ms = ms[FPL_KTAG_FP64];
-    if (runs) *runs = (int)ctx->prof_runs;
-    ctx->prof_tag.clear();
-    ctx->prof_runs = 0;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx) return FPL_ERR_NULL;
+        double ms[FPL_KTAG_COUNT] = {};
+        for (size_t p = 0; p < ctx->prof_tag.size(); ++p) {
+            FPL_CUDA(ctx, cudaEventSynchronize(ctx->prof_ev[2 * p + 1]));
+            float x = 0.f;
+            FPL_CUDA(ctx, cudaEventElapsedTime(&x, ctx->prof_ev[2 * p], ctx->prof_ev[2 * p + 1]));
+            ms[ctx->prof_tag[p]] += x;
+        }
+        for (int t = 0; t < FPL_KTAG_COUNT; ++t) ctx->prof_ms[t] = ms[t];
+        if (fp32_ms) *fp32_ms = ms[FPL_KTAG_FP32] + ms[FPL_KTAG_GRAM] + ms[FPL_KTAG_SOLVE];
+        if (fp64_ms) *fp64_ms = ms[FPL_KTAG_FP64];
+        if (runs) *runs = (int)ctx->prof_runs;
+        ctx->prof_tag.clear();
+        ctx->prof_runs = 0;
+        return FPL_OK;
+    });
 }
 
 int fpl_ctx_profile_kernels(const fpl_ctx *ctx, double *ms, int count)
 {
-    if (!ctx || !ms) return FPL_ERR_NULL;
-    for (int t = 0; t < count && t < FPL_KTAG_COUNT; ++t) ms[t] = ctx->prof_ms[t];
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx || !ms) return FPL_ERR_NULL;
+        for (int t = 0; t < count && t < FPL_KTAG_COUNT; ++t) ms[t] = ctx->prof_ms[t];
+        return FPL_OK;
+    });
 }
 
 }  // extern "C"

@@ -31,6 +31,7 @@
 #include "batch.h"
 #include "ctx.h"
 #include "fringe_gb300.h"
+#include "guard.h"
 #include "kernels.h"
 #include "pixel.cuh"
 
@@ -342,380 +343,388 @@ extern "C" {
 
 int fpl_batch_destroy(fpl_batch *b)
 {
-    if (!b) return FPL_OK;
-    if (b->ctx) cudaSetDevice(b->ctx->device);
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
-    if (b->d_table) cudaFree(b->d_table);
-    if (b->d_scratch) cudaFree(b->d_scratch);
-    if (b->d_segs) cudaFree(b->d_segs);
-    if (b->d_ments) cudaFree(b->d_ments);
-    if (b->d_m64) cudaFree(b->d_m64);
-    if (b->d_rec) cudaFree(b->d_rec);
-    delete b;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!b) return FPL_OK;
+        if (b->ctx) cudaSetDevice(b->ctx->device);
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+        if (b->d_table) cudaFree(b->d_table);
+        if (b->d_scratch) cudaFree(b->d_scratch);
+        if (b->d_segs) cudaFree(b->d_segs);
+        if (b->d_ments) cudaFree(b->d_ments);
+        if (b->d_m64) cudaFree(b->d_m64);
+        if (b->d_rec) cudaFree(b->d_rec);
+        delete b;
+        return FPL_OK;
+    });
 }
 
 int fpl_batch_create(fpl_ctx *ctx, const fpl_job *jobs, int njobs, int flags, fpl_batch **out)
 {
-    if (!ctx || !jobs || !out || njobs <= 0) return FPL_ERR_NULL;
-    *out = nullptr;
-    for (int j = 0; j < njobs; ++j) {
-        int rc = fpl_validate_job(&jobs[j]);
-        if (rc) return rc;
-        if (jobs[j].memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
-    }
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return FPL_ERR_CUDA;
-    fpl_batch *b = new fpl_batch();
-    b->ctx = ctx;
-    b->njobs = njobs;
-    auto is_mixed = [&](const fpl_job &jb) {
-        return jb.precision == FPL_PREC_MIXED && fpl::gram_box_supported(jb.nbands, jb.half_window_y, jb.half_window_x);
-    };
-    // FP32 jobs, grouped by padded depth
-    std::vector<int> order;
-    for (int j = 0; j < njobs; ++j)
-        if (!is_mixed(jobs[j])) order.push_back(j);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int c) { return fpl::pick_np(jobs[a].nbands) < fpl::pick_np(jobs[c].nbands); });
-    const int nf = (int)order.size();
-    // mixed jobs: row pieces of at most kWavePx pixels, packed into waves
-    struct Piece { int job, ra, rb; long long px; };
-    const long long kWavePx = 1ll << 20;
-    std::vector<Piece> pieces;
-    for (int j = 0; j < njobs; ++j) {
-        if (!is_mixed(jobs[j])) continue;
-        const fpl_job &jb = jobs[j];
-        const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
-        const int step = (int)std::max<long long>(1, kWavePx / jb.cols);
-        for (int ra = r0; ra < r1; ra += step) {
-            const int rb = std::min(r1, ra + step);
-            pieces.push_back({j, ra, rb, (long long)(rb - ra) * jb.cols});
+    return fpl_guard([&]() -> int {
+        if (!ctx || !jobs || !out || njobs <= 0) return FPL_ERR_NULL;
+        *out = nullptr;
+        for (int j = 0; j < njobs; ++j) {
+            int rc = fpl_validate_job(&jobs[j]);
+            if (rc) return rc;
+            if (jobs[j].memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
         }
-    }
-    const int np_ = (int)pieces.size();
-    b->nent = nf + np_;
-    long long fb_total = 0;
-    for (int j = 0; j < njobs; ++j) {
-        const fpl_job &jb = jobs[j];
-        const int r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
-        fb_total += (long long)(r1 - jb.row_begin) * jb.cols;
-    }
-    b->pixels = fb_total;
-    // scratch: per-entry counters | work counters (one per class, <= 3) | FP64 lists
-    b->counter_bytes = kJobCounterBytes * b->nent + 64;
-    const size_t scratch = b->counter_bytes + sizeof(long long) * (size_t)std::max<long long>(fb_total, 1);
-    if (cudaMalloc(&b->d_scratch, scratch) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_NOMEM; }
-    std::vector<fpl::BatchEntry> table(nf);
-    long long fb_off = 0;
-    char *cnt_base = static_cast<char *>(b->d_scratch);
-    long long *lists = reinterpret_cast<long long *>(cnt_base + b->counter_bytes);
-    auto set_counters = [&](fpl::KParams &P, int e) {
-        P.fb_count = reinterpret_cast<int *>(cnt_base + kJobCounterBytes * e);
-        P.err = reinterpret_cast<unsigned *>(cnt_base + kJobCounterBytes * e + 16);
-        P.slow = reinterpret_cast<int *>(cnt_base + kJobCounterBytes * e + 32);
-        P.fb_list = lists + fb_off;
-        P.fb_cap = (int)std::min<long long>(P.npix, 0x7fffffff);
-        fb_off += P.npix;
-    };
-    for (int e = 0; e < nf; ++e) {
-        const int j = order[e];
-        const fpl_job &jb = jobs[j];
-        const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
-        fpl::KParams &P = table[e].P;
-        fpl::fill_params(P, jb, r0, r1, ctx->amb_scale, ctx->cond_max);
-        P.shift = ctx->shift;
-        P.shift_backoff = ctx->shift_backoff;
-        set_counters(P, e);
-        b->job_of_entry.push_back(j);
-    }
-    // mixed pieces: parameters, waves, records buffer
-    if (np_ > 0) {
-        std::vector<fpl::KParams> pp(np_);
-        std::vector<int> wave_of(np_);
-        std::vector<long long> rec_off(np_), info_off(np_);
-        size_t rec_max = 0, info_max = 0;
-        {
-            long long wpx = 0;
-            size_t rec = 0, inf = 0;
-            int w = -1;
+        if (cudaSetDevice(ctx->device) != cudaSuccess) return FPL_ERR_CUDA;
+        fpl_batch *b = new fpl_batch();
+        b->ctx = ctx;
+        b->njobs = njobs;
+        auto is_mixed = [&](const fpl_job &jb) {
+            return jb.precision == FPL_PREC_MIXED && fpl::gram_box_supported(jb.nbands, jb.half_window_y, jb.half_window_x);
+        };
+        // FP32 jobs, grouped by padded depth
+        std::vector<int> order;
+        for (int j = 0; j < njobs; ++j)
+            if (!is_mixed(jobs[j])) order.push_back(j);
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int c) { return fpl::pick_np(jobs[a].nbands) < fpl::pick_np(jobs[c].nbands); });
+        const int nf = (int)order.size();
+        // mixed jobs: row pieces of at most kWavePx pixels, packed into waves
+        struct Piece { int job, ra, rb; long long px; };
+        const long long kWavePx = 1ll << 20;
+        std::vector<Piece> pieces;
+        for (int j = 0; j < njobs; ++j) {
+            if (!is_mixed(jobs[j])) continue;
+            const fpl_job &jb = jobs[j];
+            const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
+            const int step = (int)std::max<long long>(1, kWavePx / jb.cols);
+            for (int ra = r0; ra < r1; ra += step) {
+                const int rb = std::min(r1, ra + step);
+                pieces.push_back({j, ra, rb, (long long)(rb - ra) * jb.cols});
+            }
+        }
+        const int np_ = (int)pieces.size();
+        b->nent = nf + np_;
+        long long fb_total = 0;
+        for (int j = 0; j < njobs; ++j) {
+            const fpl_job &jb = jobs[j];
+            const int r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
+            fb_total += (long long)(r1 - jb.row_begin) * jb.cols;
+        }
+        b->pixels = fb_total;
+        // scratch: per-entry counters | work counters (one per class, <= 3) | FP64 lists
+        b->counter_bytes = kJobCounterBytes * b->nent + 64;
+        const size_t scratch = b->counter_bytes + sizeof(long long) * (size_t)std::max<long long>(fb_total, 1);
+        if (cudaMalloc(&b->d_scratch, scratch) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_NOMEM; }
+        std::vector<fpl::BatchEntry> table(nf);
+        long long fb_off = 0;
+        char *cnt_base = static_cast<char *>(b->d_scratch);
+        long long *lists = reinterpret_cast<long long *>(cnt_base + b->counter_bytes);
+        auto set_counters = [&](fpl::KParams &P, int e) {
+            P.fb_count = reinterpret_cast<int *>(cnt_base + kJobCounterBytes * e);
+            P.err = reinterpret_cast<unsigned *>(cnt_base + kJobCounterBytes * e + 16);
+            P.slow = reinterpret_cast<int *>(cnt_base + kJobCounterBytes * e + 32);
+            P.fb_list = lists + fb_off;
+            P.fb_cap = (int)std::min<long long>(P.npix, 0x7fffffff);
+            fb_off += P.npix;
+        };
+        for (int e = 0; e < nf; ++e) {
+            const int j = order[e];
+            const fpl_job &jb = jobs[j];
+            const int r0 = jb.row_begin, r1 = jb.row_end <= 0 ? jb.rows : jb.row_end;
+            fpl::KParams &P = table[e].P;
+            fpl::fill_params(P, jb, r0, r1, ctx->amb_scale, ctx->cond_max);
+            P.shift = ctx->shift;
+            P.shift_backoff = ctx->shift_backoff;
+            set_counters(P, e);
+            b->job_of_entry.push_back(j);
+        }
+        // mixed pieces: parameters, waves, records buffer
+        if (np_ > 0) {
+            std::vector<fpl::KParams> pp(np_);
+            std::vector<int> wave_of(np_);
+            std::vector<long long> rec_off(np_), info_off(np_);
+            size_t rec_max = 0, info_max = 0;
+            {
+                long long wpx = 0;
+                size_t rec = 0, inf = 0;
+                int w = -1;
+                for (int i = 0; i < np_; ++i) {
+                    const Piece &pc = pieces[i];
+                    const fpl_job &jb = jobs[pc.job];
+                    if (w < 0 || wpx + pc.px > kWavePx) { ++w; wpx = 0; rec = 0; inf = 0; }
+                    wave_of[i] = w;
+                    wpx += pc.px;
+                    const int cstride = fpl::gram_box_record(jb.nbands);
+                    rec_off[i] = (long long)rec;
+                    info_off[i] = (long long)inf;
+                    rec += (size_t)pc.px * cstride;
+                    inf += (size_t)pc.px;
+                    rec_max = std::max(rec_max, rec);
+                    info_max = std::max(info_max, inf);
+                }
+                b->waves.resize(w + 1);
+            }
+            const size_t rec_bytes = (sizeof(float) * rec_max + 255) & ~size_t(255);
+            if (cudaMalloc(&b->d_rec, rec_bytes + sizeof(int) * std::max<size_t>(info_max, 1)) != cudaSuccess) {
+                fpl_batch_destroy(b);
+                return FPL_ERR_NOMEM;
+            }
+            float *recs = static_cast<float *>(b->d_rec);
+            int *infos = reinterpret_cast<int *>(static_cast<char *>(b->d_rec) + rec_bytes);
             for (int i = 0; i < np_; ++i) {
                 const Piece &pc = pieces[i];
                 const fpl_job &jb = jobs[pc.job];
-                if (w < 0 || wpx + pc.px > kWavePx) { ++w; wpx = 0; rec = 0; inf = 0; }
-                wave_of[i] = w;
-                wpx += pc.px;
-                const int cstride = fpl::gram_box_record(jb.nbands);
-                rec_off[i] = (long long)rec;
-                info_off[i] = (long long)inf;
-                rec += (size_t)pc.px * cstride;
-                inf += (size_t)pc.px;
-                rec_max = std::max(rec_max, rec);
-                info_max = std::max(info_max, inf);
+                fpl::KParams &P = pp[i];
+                fpl::fill_params(P, jb, pc.ra, pc.rb, ctx->amb_scale, ctx->cond_max);
+                P.shift = ctx->shift;
+                P.shift_backoff = ctx->shift_backoff;
+                set_counters(P, nf + i);
+                P.cbuf = reinterpret_cast<float2 *>(recs + rec_off[i]);
+                P.cinfo = infos + info_off[i];
+                P.cbase = P.pix_begin;
+                P.cstride = fpl::gram_box_record(jb.nbands);
+                b->job_of_entry.push_back(pc.job);
             }
-            b->waves.resize(w + 1);
-        }
-        const size_t rec_bytes = (sizeof(float) * rec_max + 255) & ~size_t(255);
-        if (cudaMalloc(&b->d_rec, rec_bytes + sizeof(int) * std::max<size_t>(info_max, 1)) != cudaSuccess) {
-            fpl_batch_destroy(b);
-            return FPL_ERR_NOMEM;
-        }
-        float *recs = static_cast<float *>(b->d_rec);
-        int *infos = reinterpret_cast<int *>(static_cast<char *>(b->d_rec) + rec_bytes);
-        for (int i = 0; i < np_; ++i) {
-            const Piece &pc = pieces[i];
-            const fpl_job &jb = jobs[pc.job];
-            fpl::KParams &P = pp[i];
-            fpl::fill_params(P, jb, pc.ra, pc.rb, ctx->amb_scale, ctx->cond_max);
-            P.shift = ctx->shift;
-            P.shift_backoff = ctx->shift_backoff;
-            set_counters(P, nf + i);
-            P.cbuf = reinterpret_cast<float2 *>(recs + rec_off[i]);
-            P.cinfo = infos + info_off[i];
-            P.cbase = P.pix_begin;
-            P.cstride = fpl::gram_box_record(jb.nbands);
-            b->job_of_entry.push_back(pc.job);
-        }
-        // per wave: Gamma segments, entries by padded depth
-        std::vector<fpl::BoxSeg> segs;
-        std::vector<fpl::BatchEntry> ments;
-        for (size_t w = 0; w < b->waves.size(); ++w) {
-            MixedWave &mw = b->waves[w];
-            mw.seg_first = (int)segs.size();
-            for (int i = 0; i < np_; ++i) {
-                if (wave_of[i] != (int)w) continue;
-                fpl::BoxSeg sg;
-                sg.P = pp[i];
-                sg.tile_offset = mw.seg_tiles;
-                mw.seg_tiles += fpl::gram_box_tiles(pp[i]);
-                mw.seg_smem = std::max(mw.seg_smem, fpl::gram_box_smem(pp[i].nb, pp[i].ny, pp[i].nx));
-                segs.push_back(sg);
+            // per wave: Gamma segments, entries by padded depth
+            std::vector<fpl::BoxSeg> segs;
+            std::vector<fpl::BatchEntry> ments;
+            for (size_t w = 0; w < b->waves.size(); ++w) {
+                MixedWave &mw = b->waves[w];
+                mw.seg_first = (int)segs.size();
+                for (int i = 0; i < np_; ++i) {
+                    if (wave_of[i] != (int)w) continue;
+                    fpl::BoxSeg sg;
+                    sg.P = pp[i];
+                    sg.tile_offset = mw.seg_tiles;
+                    mw.seg_tiles += fpl::gram_box_tiles(pp[i]);
+                    mw.seg_smem = std::max(mw.seg_smem, fpl::gram_box_smem(pp[i].nb, pp[i].ny, pp[i].nx));
+                    segs.push_back(sg);
+                }
+                mw.seg_count = (int)segs.size() - mw.seg_first;
+                for (int c = 0; c < 3; ++c) {
+                    const int npd = 16 << c;
+                    mw.ent_first[c] = (int)ments.size();
+                    for (int i = 0; i < np_; ++i) {
+                        if (wave_of[i] != (int)w || fpl::pick_np(pp[i].nb) != npd) continue;
+                        fpl::BatchEntry en;
+                        en.P = pp[i];
+                        en.px_offset = mw.ent_total[c];
+                        mw.ent_total[c] += pp[i].npix;
+                        ments.push_back(en);
+                    }
+                    mw.ent_count[c] = (int)ments.size() - mw.ent_first[c];
+                }
             }
-            mw.seg_count = (int)segs.size() - mw.seg_first;
+            // FP64 settle table: every piece, by padded depth
+            std::vector<fpl::BatchEntry> m64;
             for (int c = 0; c < 3; ++c) {
                 const int npd = 16 << c;
-                mw.ent_first[c] = (int)ments.size();
+                b->m64_first[c] = (int)m64.size();
                 for (int i = 0; i < np_; ++i) {
-                    if (wave_of[i] != (int)w || fpl::pick_np(pp[i].nb) != npd) continue;
+                    if (fpl::pick_np(pp[i].nb) != npd) continue;
                     fpl::BatchEntry en;
                     en.P = pp[i];
-                    en.px_offset = mw.ent_total[c];
-                    mw.ent_total[c] += pp[i].npix;
-                    ments.push_back(en);
+                    en.px_offset = 0;
+                    m64.push_back(en);
                 }
-                mw.ent_count[c] = (int)ments.size() - mw.ent_first[c];
+                b->m64_count[c] = (int)m64.size() - b->m64_first[c];
+                if (b->m64_count[c] && fpl::configure_np(npd) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
             }
-        }
-        // FP64 settle table: every piece, by padded depth
-        std::vector<fpl::BatchEntry> m64;
-        for (int c = 0; c < 3; ++c) {
-            const int npd = 16 << c;
-            b->m64_first[c] = (int)m64.size();
-            for (int i = 0; i < np_; ++i) {
-                if (fpl::pick_np(pp[i].nb) != npd) continue;
-                fpl::BatchEntry en;
-                en.P = pp[i];
-                en.px_offset = 0;
-                m64.push_back(en);
+            if (cudaMalloc(&b->d_segs, sizeof(fpl::BoxSeg) * std::max<size_t>(segs.size(), 1)) != cudaSuccess ||
+                cudaMalloc(&b->d_ments, sizeof(fpl::BatchEntry) * std::max<size_t>(ments.size(), 1)) != cudaSuccess ||
+                cudaMalloc(&b->d_m64, sizeof(fpl::BatchEntry) * std::max<size_t>(m64.size(), 1)) != cudaSuccess) {
+                fpl_batch_destroy(b);
+                return FPL_ERR_NOMEM;
             }
-            b->m64_count[c] = (int)m64.size() - b->m64_first[c];
-            if (b->m64_count[c] && fpl::configure_np(npd) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
+            if (cudaMemcpy(b->d_segs, segs.data(), sizeof(fpl::BoxSeg) * segs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemcpy(b->d_ments, ments.data(), sizeof(fpl::BatchEntry) * ments.size(), cudaMemcpyHostToDevice) !=
+                    cudaSuccess ||
+                cudaMemcpy(b->d_m64, m64.data(), sizeof(fpl::BatchEntry) * m64.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+                fpl_batch_destroy(b);
+                return FPL_ERR_CUDA;
+            }
+            // kernel attributes are set before any capture
+            for (int c = 0; c < 3; ++c)
+                if (fpl::prepare_mixed_batch(16 << c) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
         }
-        if (cudaMalloc(&b->d_segs, sizeof(fpl::BoxSeg) * std::max<size_t>(segs.size(), 1)) != cudaSuccess ||
-            cudaMalloc(&b->d_ments, sizeof(fpl::BatchEntry) * std::max<size_t>(ments.size(), 1)) != cudaSuccess ||
-            cudaMalloc(&b->d_m64, sizeof(fpl::BatchEntry) * std::max<size_t>(m64.size(), 1)) != cudaSuccess) {
+        // classes and their pixel offsets
+        for (int e = 0; e < nf;) {
+            BatchClass k;
+            k.np = fpl::pick_np(table[e].P.nb);
+            k.first = e;
+            long long off = 0;
+            while (e < nf && fpl::pick_np(table[e].P.nb) == k.np) {
+                table[e].px_offset = off;
+                off += table[e].P.npix;
+                ++e;
+            }
+            k.count = e - k.first;
+            k.total = off;
+            k.warps = fpl::max_warps(k.np, false);
+            if (fpl::configure_np(k.np) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
+            b->classes.push_back(k);
+        }
+        if (cudaMalloc(&b->d_table, sizeof(fpl::BatchEntry) * std::max(nf, 1)) != cudaSuccess) {
             fpl_batch_destroy(b);
             return FPL_ERR_NOMEM;
         }
-        if (cudaMemcpy(b->d_segs, segs.data(), sizeof(fpl::BoxSeg) * segs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(b->d_ments, ments.data(), sizeof(fpl::BatchEntry) * ments.size(), cudaMemcpyHostToDevice) !=
-                cudaSuccess ||
-            cudaMemcpy(b->d_m64, m64.data(), sizeof(fpl::BatchEntry) * m64.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (nf && cudaMemcpy(b->d_table, table.data(), sizeof(fpl::BatchEntry) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
             fpl_batch_destroy(b);
             return FPL_ERR_CUDA;
         }
-        // kernel attributes are set before any capture
-        for (int c = 0; c < 3; ++c)
-            if (fpl::prepare_mixed_batch(16 << c) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
-    }
-    // classes and their pixel offsets
-    for (int e = 0; e < nf;) {
-        BatchClass k;
-        k.np = fpl::pick_np(table[e].P.nb);
-        k.first = e;
-        long long off = 0;
-        while (e < nf && fpl::pick_np(table[e].P.nb) == k.np) {
-            table[e].px_offset = off;
-            off += table[e].P.npix;
-            ++e;
+        if (cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            fpl_batch_destroy(b);
+            return FPL_ERR_CUDA;
         }
-        k.count = e - k.first;
-        k.total = off;
-        k.warps = fpl::max_warps(k.np, false);
-        if (fpl::configure_np(k.np) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
-        b->classes.push_back(k);
-    }
-    if (cudaMalloc(&b->d_table, sizeof(fpl::BatchEntry) * std::max(nf, 1)) != cudaSuccess) {
-        fpl_batch_destroy(b);
-        return FPL_ERR_NOMEM;
-    }
-    if (nf && cudaMemcpy(b->d_table, table.data(), sizeof(fpl::BatchEntry) * nf, cudaMemcpyHostToDevice) != cudaSuccess) {
-        fpl_batch_destroy(b);
-        return FPL_ERR_CUDA;
-    }
-    if (cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
-        fpl_batch_destroy(b);
-        return FPL_ERR_CUDA;
-    }
-    // autotune: warps per CTA per class, timed on the batch itself, cached per key
-    if (flags & FPL_BATCH_AUTOTUNE) {
-        unsigned long long *d_sum = nullptr;
-        if (cudaMalloc(&d_sum, sizeof(unsigned long long)) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_NOMEM; }
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        // one untimed run first: the candidates' times then exclude one-time
-        // costs (module loading, kernel attributes, first-touch of buffers)
-        if (batch_enqueue(b, b->cap_stream) != FPL_OK || cudaStreamSynchronize(b->cap_stream) != cudaSuccess) {
+        // autotune: warps per CTA per class, timed on the batch itself, cached per key
+        if (flags & FPL_BATCH_AUTOTUNE) {
+            unsigned long long *d_sum = nullptr;
+            if (cudaMalloc(&d_sum, sizeof(unsigned long long)) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_NOMEM; }
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            // one untimed run first: the candidates' times then exclude one-time
+            // costs (module loading, kernel attributes, first-touch of buffers)
+            if (batch_enqueue(b, b->cap_stream) != FPL_OK || cudaStreamSynchronize(b->cap_stream) != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                cudaFree(d_sum);
+                fpl_batch_destroy(b);
+                return FPL_ERR_CUDA;
+            }
+            for (BatchClass &k : b->classes) {
+                // key: (NP, taps of the first job, mean SHP count of the class / 16)
+                unsigned long long shp = 0, px = 0;
+                int taps = table[k.first].P.K;
+                for (int e = k.first; e < k.first + k.count; ++e) {
+                    const fpl::KParams &P = table[e].P;
+                    cudaMemsetAsync(d_sum, 0, sizeof(unsigned long long), b->cap_stream);
+                    fpl::k_popcount<<<256, 256, 0, b->cap_stream>>>(P.nmap + P.pix_begin * P.nulong,
+                                                                     P.npix * P.nulong, d_sum);
+                    unsigned long long s = 0;
+                    cudaMemcpyAsync(&s, d_sum, sizeof(s), cudaMemcpyDeviceToHost, b->cap_stream);
+                    cudaStreamSynchronize(b->cap_stream);
+                    shp += s;
+                    px += (unsigned long long)P.npix;
+                }
+                const long long key = ((long long)k.np << 40) | ((long long)taps << 16) | (long long)(px ? shp / px / 16 : 0);
+                auto it = ctx->tuned_warps.find(key);
+                if (it != ctx->tuned_warps.end()) {
+                    k.warps = it->second;
+                    continue;
+                }
+                const int wmax = fpl::max_warps(k.np, false);
+                int cands[4] = {std::max(1, wmax / 2), std::max(1, (3 * wmax) / 4), wmax, 0};
+                float best = 1e30f;
+                int best_w = wmax;
+                for (int ci = 0; ci < 3; ++ci) {
+                    const int w = cands[ci];
+                    if (ci > 0 && w == cands[ci - 1]) continue;
+                    k.warps = w;
+                    cudaEventRecord(e0, b->cap_stream);
+                    if (batch_enqueue(b, b->cap_stream) != FPL_OK) break;
+                    cudaEventRecord(e1, b->cap_stream);
+                    cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ms < best) { best = ms; best_w = w; }
+                }
+                k.warps = best_w;
+                ctx->tuned_warps[key] = best_w;
+            }
+            // mixed form: warps per CTA of the solve launches of each padded depth,
+            // keyed like the FP32 classes with a bit for the form
+            for (int c = 0; c < 3; ++c) {
+                if (!b->m64_count[c]) continue;
+                const int np = 16 << c;
+                unsigned long long shp = 0, px = 0;
+                int taps = 0;
+                std::vector<fpl::BatchEntry> pcs(b->m64_count[c]);
+                cudaMemcpy(pcs.data(), b->d_m64 + b->m64_first[c], sizeof(fpl::BatchEntry) * pcs.size(),
+                           cudaMemcpyDeviceToHost);
+                for (const fpl::BatchEntry &en : pcs) {
+                    const fpl::KParams &P = en.P;
+                    taps = std::max(taps, P.K);
+                    cudaMemsetAsync(d_sum, 0, sizeof(unsigned long long), b->cap_stream);
+                    fpl::k_popcount<<<256, 256, 0, b->cap_stream>>>(P.nmap + P.pix_begin * P.nulong,
+                                                                     P.npix * P.nulong, d_sum);
+                    unsigned long long sum = 0;
+                    cudaMemcpyAsync(&sum, d_sum, sizeof(sum), cudaMemcpyDeviceToHost, b->cap_stream);
+                    cudaStreamSynchronize(b->cap_stream);
+                    shp += sum;
+                    px += (unsigned long long)P.npix;
+                }
+                const long long key = (1ll << 62) | ((long long)np << 40) | ((long long)taps << 16) |
+                                      (long long)(px ? shp / px / 16 : 0);
+                auto it = ctx->tuned_warps.find(key);
+                if (it != ctx->tuned_warps.end()) {
+                    b->mixed_warps[c] = it->second;
+                    continue;
+                }
+                const int wmax = fpl::solve_max_warps(np);
+                const int cands[3] = {std::max(1, wmax / 2), std::max(1, (3 * wmax) / 4), wmax};
+                float best = 1e30f;
+                int best_w = wmax;
+                for (int ci = 0; ci < 3; ++ci) {
+                    const int w = cands[ci];
+                    if (ci > 0 && w == cands[ci - 1]) continue;
+                    b->mixed_warps[c] = w;
+                    cudaEventRecord(e0, b->cap_stream);
+                    if (batch_enqueue(b, b->cap_stream) != FPL_OK) break;
+                    cudaEventRecord(e1, b->cap_stream);
+                    cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ms < best) { best = ms; best_w = w; }
+                }
+                b->mixed_warps[c] = best_w;
+                ctx->tuned_warps[key] = best_w;
+            }
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             cudaFree(d_sum);
-            fpl_batch_destroy(b);
-            return FPL_ERR_CUDA;
+            if (cudaStreamSynchronize(b->cap_stream) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
         }
-        for (BatchClass &k : b->classes) {
-            // key: (NP, taps of the first job, mean SHP count of the class / 16)
-            unsigned long long shp = 0, px = 0;
-            int taps = table[k.first].P.K;
-            for (int e = k.first; e < k.first + k.count; ++e) {
-                const fpl::KParams &P = table[e].P;
-                cudaMemsetAsync(d_sum, 0, sizeof(unsigned long long), b->cap_stream);
-                fpl::k_popcount<<<256, 256, 0, b->cap_stream>>>(P.nmap + P.pix_begin * P.nulong,
-                                                                 P.npix * P.nulong, d_sum);
-                unsigned long long s = 0;
-                cudaMemcpyAsync(&s, d_sum, sizeof(s), cudaMemcpyDeviceToHost, b->cap_stream);
-                cudaStreamSynchronize(b->cap_stream);
-                shp += s;
-                px += (unsigned long long)P.npix;
+        if (flags & FPL_BATCH_GRAPH) {
+            if (cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                fpl_batch_destroy(b);
+                return FPL_ERR_CUDA;
             }
-            const long long key = ((long long)k.np << 40) | ((long long)taps << 16) | (long long)(px ? shp / px / 16 : 0);
-            auto it = ctx->tuned_warps.find(key);
-            if (it != ctx->tuned_warps.end()) {
-                k.warps = it->second;
-                continue;
+            int rc = batch_enqueue(b, b->cap_stream);
+            cudaError_t e = cudaStreamEndCapture(b->cap_stream, &b->graph);
+            if (rc || e != cudaSuccess || cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) {
+                fpl_batch_destroy(b);
+                return rc ? rc : FPL_ERR_CUDA;
             }
-            const int wmax = fpl::max_warps(k.np, false);
-            int cands[4] = {std::max(1, wmax / 2), std::max(1, (3 * wmax) / 4), wmax, 0};
-            float best = 1e30f;
-            int best_w = wmax;
-            for (int ci = 0; ci < 3; ++ci) {
-                const int w = cands[ci];
-                if (ci > 0 && w == cands[ci - 1]) continue;
-                k.warps = w;
-                cudaEventRecord(e0, b->cap_stream);
-                if (batch_enqueue(b, b->cap_stream) != FPL_OK) break;
-                cudaEventRecord(e1, b->cap_stream);
-                cudaEventSynchronize(e1);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (ms < best) { best = ms; best_w = w; }
-            }
-            k.warps = best_w;
-            ctx->tuned_warps[key] = best_w;
         }
-        // mixed form: warps per CTA of the solve launches of each padded depth,
-        // keyed like the FP32 classes with a bit for the form
-        for (int c = 0; c < 3; ++c) {
-            if (!b->m64_count[c]) continue;
-            const int np = 16 << c;
-            unsigned long long shp = 0, px = 0;
-            int taps = 0;
-            std::vector<fpl::BatchEntry> pcs(b->m64_count[c]);
-            cudaMemcpy(pcs.data(), b->d_m64 + b->m64_first[c], sizeof(fpl::BatchEntry) * pcs.size(),
-                       cudaMemcpyDeviceToHost);
-            for (const fpl::BatchEntry &en : pcs) {
-                const fpl::KParams &P = en.P;
-                taps = std::max(taps, P.K);
-                cudaMemsetAsync(d_sum, 0, sizeof(unsigned long long), b->cap_stream);
-                fpl::k_popcount<<<256, 256, 0, b->cap_stream>>>(P.nmap + P.pix_begin * P.nulong,
-                                                                 P.npix * P.nulong, d_sum);
-                unsigned long long sum = 0;
-                cudaMemcpyAsync(&sum, d_sum, sizeof(sum), cudaMemcpyDeviceToHost, b->cap_stream);
-                cudaStreamSynchronize(b->cap_stream);
-                shp += sum;
-                px += (unsigned long long)P.npix;
-            }
-            const long long key = (1ll << 62) | ((long long)np << 40) | ((long long)taps << 16) |
-                                  (long long)(px ? shp / px / 16 : 0);
-            auto it = ctx->tuned_warps.find(key);
-            if (it != ctx->tuned_warps.end()) {
-                b->mixed_warps[c] = it->second;
-                continue;
-            }
-            const int wmax = fpl::solve_max_warps(np);
-            const int cands[3] = {std::max(1, wmax / 2), std::max(1, (3 * wmax) / 4), wmax};
-            float best = 1e30f;
-            int best_w = wmax;
-            for (int ci = 0; ci < 3; ++ci) {
-                const int w = cands[ci];
-                if (ci > 0 && w == cands[ci - 1]) continue;
-                b->mixed_warps[c] = w;
-                cudaEventRecord(e0, b->cap_stream);
-                if (batch_enqueue(b, b->cap_stream) != FPL_OK) break;
-                cudaEventRecord(e1, b->cap_stream);
-                cudaEventSynchronize(e1);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (ms < best) { best = ms; best_w = w; }
-            }
-            b->mixed_warps[c] = best_w;
-            ctx->tuned_warps[key] = best_w;
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        cudaFree(d_sum);
-        if (cudaStreamSynchronize(b->cap_stream) != cudaSuccess) { fpl_batch_destroy(b); return FPL_ERR_CUDA; }
-    }
-    if (flags & FPL_BATCH_GRAPH) {
-        if (cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-            fpl_batch_destroy(b);
-            return FPL_ERR_CUDA;
-        }
-        int rc = batch_enqueue(b, b->cap_stream);
-        cudaError_t e = cudaStreamEndCapture(b->cap_stream, &b->graph);
-        if (rc || e != cudaSuccess || cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) {
-            fpl_batch_destroy(b);
-            return rc ? rc : FPL_ERR_CUDA;
-        }
-    }
-    *out = b;
-    return FPL_OK;
+        *out = b;
+        return FPL_OK;
+    });
 }
 
 int fpl_batch_run(fpl_batch *b, void *stream)
 {
-    if (!b) return FPL_ERR_NULL;
-    if (cudaSetDevice(b->ctx->device) != cudaSuccess) return FPL_ERR_CUDA;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (b->exec) return cudaGraphLaunch(b->exec, st) == cudaSuccess ? FPL_OK : FPL_ERR_CUDA;
-    return batch_enqueue(b, st);
+    return fpl_guard([&]() -> int {
+        if (!b) return FPL_ERR_NULL;
+        if (cudaSetDevice(b->ctx->device) != cudaSuccess) return FPL_ERR_CUDA;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        if (b->exec) return cudaGraphLaunch(b->exec, st) == cudaSuccess ? FPL_OK : FPL_ERR_CUDA;
+        return batch_enqueue(b, st);
+    });
 }
 
 int fpl_batch_stats(const fpl_batch *b, fpl_stats *out)
 {
-    if (!b || !out) return FPL_ERR_NULL;
-    std::vector<int> c(b->counter_bytes / sizeof(int));
-    if (cudaMemcpy(c.data(), b->d_scratch, b->counter_bytes, cudaMemcpyDeviceToHost) != cudaSuccess) return FPL_ERR_CUDA;
-    std::memset(out, 0, sizeof(*out));
-    out->pixels = b->pixels;
-    unsigned err = 0;
-    for (int e = 0; e < b->nent; ++e) {
-        out->fp64_pixels += c[(kJobCounterBytes / sizeof(int)) * e];
-        err |= (unsigned)c[(kJobCounterBytes / sizeof(int)) * e + 4];
-        out->slow_path_pixels += c[(kJobCounterBytes / sizeof(int)) * e + 8];
-    }
-    return err ? FPL_ERR_DEVICE_CHECK : FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!b || !out) return FPL_ERR_NULL;
+        std::vector<int> c(b->counter_bytes / sizeof(int));
+        if (cudaMemcpy(c.data(), b->d_scratch, b->counter_bytes, cudaMemcpyDeviceToHost) != cudaSuccess) return FPL_ERR_CUDA;
+        std::memset(out, 0, sizeof(*out));
+        out->pixels = b->pixels;
+        unsigned err = 0;
+        for (int e = 0; e < b->nent; ++e) {
+            out->fp64_pixels += c[(kJobCounterBytes / sizeof(int)) * e];
+            err |= (unsigned)c[(kJobCounterBytes / sizeof(int)) * e + 4];
+            out->slow_path_pixels += c[(kJobCounterBytes / sizeof(int)) * e + 8];
+        }
+        return err ? FPL_ERR_DEVICE_CHECK : FPL_OK;
+    });
 }
 
 }  // extern "C"

@@ -15,6 +15,7 @@
 #include <string>
 
 #include "fringe_gb300.h"
+#include "guard.h"
 #include "ctx.h"
 
 namespace {
@@ -75,24 +76,26 @@ __global__ void k_integrate_ps(const float2 *__restrict__ ds, const float2 *__re
 
 extern "C" int fpl_integrate_ps(fpl_ctx *ctx, const fpl_ps_job *job, void *stream)
 {
-    if (!ctx || !job) return FPL_ERR_NULL;
-    if (job->rows < 0 || job->cols < 0 || job->nbands < 1 || job->master < 0 || job->master >= job->nbands)
-        return FPL_ERR_OPTIONS;
-    const long long npix = (long long)job->rows * job->cols;
-    if (npix == 0) return FPL_OK;             // empty scene: no buffer is touched
-    if (!job->ds || !job->slc || !job->tcorr || !job->ps || !job->tcorr_out || (job->nbands > 1 && !job->ifg))
-        return FPL_ERR_NULL;
-    cudaError_t e = cudaSetDevice(ctx->device);
-    if (e == cudaSuccess) {
-        const long long blocks = std::min<long long>((npix + 255) / 256, (long long)ctx->num_sms * 8);
-        k_integrate_ps<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-            static_cast<const float2 *>(job->ds), static_cast<const float2 *>(job->slc), job->tcorr, job->ps,
-            static_cast<float2 *>(job->ifg), job->tcorr_out, job->nbands, job->master, npix);
-        e = cudaGetLastError();
-    }
-    if (e != cudaSuccess) {
-        ctx->last_error = std::string("fpl_integrate_ps: ") + cudaGetErrorString(e);
-        return FPL_ERR_CUDA;
-    }
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!ctx || !job) return FPL_ERR_NULL;
+        if (job->rows < 0 || job->cols < 0 || job->nbands < 1 || job->master < 0 || job->master >= job->nbands)
+            return FPL_ERR_OPTIONS;
+        const long long npix = (long long)job->rows * job->cols;
+        if (npix == 0) return FPL_OK;             // empty scene: no buffer is touched
+        if (!job->ds || !job->slc || !job->tcorr || !job->ps || !job->tcorr_out || (job->nbands > 1 && !job->ifg))
+            return FPL_ERR_NULL;
+        cudaError_t e = cudaSetDevice(ctx->device);
+        if (e == cudaSuccess) {
+            const long long blocks = std::min<long long>((npix + 255) / 256, (long long)ctx->num_sms * 8);
+            k_integrate_ps<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+                static_cast<const float2 *>(job->ds), static_cast<const float2 *>(job->slc), job->tcorr, job->ps,
+                static_cast<float2 *>(job->ifg), job->tcorr_out, job->nbands, job->master, npix);
+            e = cudaGetLastError();
+        }
+        if (e != cudaSuccess) {
+            ctx->last_error = std::string("fpl_integrate_ps: ") + cudaGetErrorString(e);
+            return FPL_ERR_CUDA;
+        }
+        return FPL_OK;
+    });
 }

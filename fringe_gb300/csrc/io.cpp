@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "fringe_gb300.h"
+#include "guard.h"
 
 namespace {
 
@@ -435,208 +436,210 @@ void fpl_options_default(fpl_options *o)
 
 int fpl_process(const fpl_options *opts)
 {
-    if (!opts || !opts->inputDS || !opts->wtsDS || !opts->outputFolder) return FPL_ERR_OPTIONS;
-    const bool verbose = opts->verbose != 0;
-    const std::string method = opts->method ? opts->method : "MLE";
-    int meth;
-    if (method == "MLE") meth = FPL_METHOD_MLE;
-    else if (method == "EVD") meth = FPL_METHOD_EVD;
-    else if (method == "STBAS") meth = FPL_METHOD_STBAS;
-    else return FPL_ERR_OPTIONS;
-    const int Ny = opts->Ny, Nx = opts->Nx;
-    const int nulong = (int)std::ceil(((2 * Ny + 1) * (2 * Nx + 1)) / 32.0);   // evd.cpp:47-48
+    return fpl_guard([&]() -> int {
+        if (!opts || !opts->inputDS || !opts->wtsDS || !opts->outputFolder) return FPL_ERR_OPTIONS;
+        const bool verbose = opts->verbose != 0;
+        const std::string method = opts->method ? opts->method : "MLE";
+        int meth;
+        if (method == "MLE") meth = FPL_METHOD_MLE;
+        else if (method == "EVD") meth = FPL_METHOD_EVD;
+        else if (method == "STBAS") meth = FPL_METHOD_STBAS;
+        else return FPL_ERR_OPTIONS;
+        const int Ny = opts->Ny, Nx = opts->Nx;
+        const int nulong = (int)std::ceil(((2 * Ny + 1) * (2 * Nx + 1)) / 32.0);   // evd.cpp:47-48
 
-    // ---- stack (evd.cpp:51-71) ----
-    std::string vrt;
-    std::string in = opts->inputDS;
-    if (!read_text(in, vrt) || lower(vrt).find("<vrtdataset") == std::string::npos) {
-        if (verbose) std::printf("Cannot open stack file { %s } for reading (a VRT is expected)\n", in.c_str());
-        return FPL_ERR_OPEN_STACK;
-    }
-    auto ds = xml_find(vrt, "VRTDataset");
-    std::string xs, ys;
-    if (ds.empty() || !xml_attr(ds[0].attrs, "rasterXSize", xs) || !xml_attr(ds[0].attrs, "rasterYSize", ys))
-        return FPL_ERR_OPEN_STACK;
-    const int cols = std::atoi(xs.c_str()), rows = std::atoi(ys.c_str());
-    const int nbands = (int)xml_find(vrt, "VRTRasterBand").size();
-    if (cols <= 0 || rows <= 0 || nbands <= 0) return FPL_ERR_OPEN_STACK;
-    if (verbose) std::printf("Number of rows  = %d\nNumber of cols  = %d\nNumber of bands = %d\n", rows, cols, nbands);
-
-    // ---- STBAS bandwidth (evd.cpp:74-91) ----
-    if (meth == FPL_METHOD_STBAS) {
-        if (opts->bandWidth <= 0 || opts->bandWidth >= nbands - 1) return FPL_ERR_OPTIONS;
-    }
-    if (opts->miniStackCount < 1 || opts->miniStackCount > nbands) return FPL_ERR_OPTIONS;
-    if (nbands > FPL_MAX_BANDS || nulong > FPL_MAX_NULONG) return FPL_ERR_UNSUPPORTED;
-
-    // ---- weights (evd.cpp:93-166) ----
-    std::string wts = opts->wtsDS;
-    std::string whdr = find_envi_header(wts);
-    EnviHeader wh;
-    if (whdr.empty() || !parse_envi_header(whdr, wh)) {
-        if (verbose) std::printf("Could not open weights dataset {%s}\n", wts.c_str());
-        return FPL_ERR_OPEN_WEIGHTS;
-    }
-    {
-        int code = 0;
-        if (wh.samples != cols) code = FPL_ERR_WIDTH;
-        if (wh.lines != rows) code = FPL_ERR_LENGTH;
-        if (wh.bands != nulong) code = FPL_ERR_NULONG;
-        int inNx = 0, inNy = 0;
-        for (auto &kv : wh.items) {
-            if (kv.first == "halfwindowx") inNx = std::atoi(kv.second.c_str());
-            if (kv.first == "halfwindowy") inNy = std::atoi(kv.second.c_str());
+        // ---- stack (evd.cpp:51-71) ----
+        std::string vrt;
+        std::string in = opts->inputDS;
+        if (!read_text(in, vrt) || lower(vrt).find("<vrtdataset") == std::string::npos) {
+            if (verbose) std::printf("Cannot open stack file { %s } for reading (a VRT is expected)\n", in.c_str());
+            return FPL_ERR_OPEN_STACK;
         }
-        if (inNx != Nx || inNx == 0) code = FPL_ERR_HALFWINDOWX;
-        if (inNy != Ny || inNy == 0) code = FPL_ERR_HALFWINDOWY;
-        if (envi_type_bytes(wh.data_type) != 4) code = code ? code : FPL_ERR_OPEN_WEIGHTS;
-        if (code) {
-            if (verbose) std::printf("Exiting with error code ....(%d)\n", code);
-            return code;
-        }
-    }
-    std::vector<RawBand> wband(1);
-    // nulong words per pixel, interleaved: read them as one BIP "band" of nulong*4 bytes
-    if (!envi_band(wts, wh, 0, wband[0])) return FPL_ERR_OPEN_WEIGHTS;
-    if (lower(wh.interleave) != "bip") {
-        if (verbose) std::printf("Weights dataset must be BIP interleaved\n");
-        return FPL_ERR_OPEN_WEIGHTS;
-    }
-    wband[0].bytes = 4 * nulong;
-    wband[0].pixel_offset = 4LL * nulong;
+        auto ds = xml_find(vrt, "VRTDataset");
+        std::string xs, ys;
+        if (ds.empty() || !xml_attr(ds[0].attrs, "rasterXSize", xs) || !xml_attr(ds[0].attrs, "rasterYSize", ys))
+            return FPL_ERR_OPEN_STACK;
+        const int cols = std::atoi(xs.c_str()), rows = std::atoi(ys.c_str());
+        const int nbands = (int)xml_find(vrt, "VRTRasterBand").size();
+        if (cols <= 0 || rows <= 0 || nbands <= 0) return FPL_ERR_OPEN_STACK;
+        if (verbose) std::printf("Number of rows  = %d\nNumber of cols  = %d\nNumber of bands = %d\n", rows, cols, nbands);
 
-    // ---- dates (evd.cpp:210-223) and band sources ----
-    std::vector<std::string> dates(nbands);
-    std::vector<RawBand> bands(nbands);
-    {
-        auto vb = xml_find(vrt, "VRTRasterBand");
-        for (int b = 0; b < nbands; ++b) {
-            std::string date;
-            for (auto &md : xml_find(vb[b].body, "Metadata")) {
-                std::string dom;
-                if (!xml_attr(md.attrs, "domain", dom) || dom != "slc") continue;
-                for (auto &mdi : xml_find(md.body, "MDI")) {
-                    std::string key;
-                    if (xml_attr(mdi.attrs, "key", key) && key == "Date") date = trim(mdi.body);
+        // ---- STBAS bandwidth (evd.cpp:74-91) ----
+        if (meth == FPL_METHOD_STBAS) {
+            if (opts->bandWidth <= 0 || opts->bandWidth >= nbands - 1) return FPL_ERR_OPTIONS;
+        }
+        if (opts->miniStackCount < 1 || opts->miniStackCount > nbands) return FPL_ERR_OPTIONS;
+        if (nbands > FPL_MAX_BANDS || nulong > FPL_MAX_NULONG) return FPL_ERR_UNSUPPORTED;
+
+        // ---- weights (evd.cpp:93-166) ----
+        std::string wts = opts->wtsDS;
+        std::string whdr = find_envi_header(wts);
+        EnviHeader wh;
+        if (whdr.empty() || !parse_envi_header(whdr, wh)) {
+            if (verbose) std::printf("Could not open weights dataset {%s}\n", wts.c_str());
+            return FPL_ERR_OPEN_WEIGHTS;
+        }
+        {
+            int code = 0;
+            if (wh.samples != cols) code = FPL_ERR_WIDTH;
+            if (wh.lines != rows) code = FPL_ERR_LENGTH;
+            if (wh.bands != nulong) code = FPL_ERR_NULONG;
+            int inNx = 0, inNy = 0;
+            for (auto &kv : wh.items) {
+                if (kv.first == "halfwindowx") inNx = std::atoi(kv.second.c_str());
+                if (kv.first == "halfwindowy") inNy = std::atoi(kv.second.c_str());
+            }
+            if (inNx != Nx || inNx == 0) code = FPL_ERR_HALFWINDOWX;
+            if (inNy != Ny || inNy == 0) code = FPL_ERR_HALFWINDOWY;
+            if (envi_type_bytes(wh.data_type) != 4) code = code ? code : FPL_ERR_OPEN_WEIGHTS;
+            if (code) {
+                if (verbose) std::printf("Exiting with error code ....(%d)\n", code);
+                return code;
+            }
+        }
+        std::vector<RawBand> wband(1);
+        // nulong words per pixel, interleaved: read them as one BIP "band" of nulong*4 bytes
+        if (!envi_band(wts, wh, 0, wband[0])) return FPL_ERR_OPEN_WEIGHTS;
+        if (lower(wh.interleave) != "bip") {
+            if (verbose) std::printf("Weights dataset must be BIP interleaved\n");
+            return FPL_ERR_OPEN_WEIGHTS;
+        }
+        wband[0].bytes = 4 * nulong;
+        wband[0].pixel_offset = 4LL * nulong;
+
+        // ---- dates (evd.cpp:210-223) and band sources ----
+        std::vector<std::string> dates(nbands);
+        std::vector<RawBand> bands(nbands);
+        {
+            auto vb = xml_find(vrt, "VRTRasterBand");
+            for (int b = 0; b < nbands; ++b) {
+                std::string date;
+                for (auto &md : xml_find(vb[b].body, "Metadata")) {
+                    std::string dom;
+                    if (!xml_attr(md.attrs, "domain", dom) || dom != "slc") continue;
+                    for (auto &mdi : xml_find(md.body, "MDI")) {
+                        std::string key;
+                        if (xml_attr(mdi.attrs, "key", key) && key == "Date") date = trim(mdi.body);
+                    }
                 }
+                if (date.size() != 8) {
+                    if (verbose) std::printf("Band %d does not appear to have Date information in slc metadata domain \n", b + 1);
+                    return FPL_ERR_DATE;
+                }
+                dates[b] = date;
+                if (!resolve_vrt_band(in, vrt, b, bands[b], 0)) {
+                    if (verbose) std::printf("Cannot resolve the source of band %d\n", b + 1);
+                    return FPL_ERR_OPEN_STACK;
+                }
+                if (bands[b].bytes != 8) return FPL_ERR_OPEN_STACK;
             }
-            if (date.size() != 8) {
-                if (verbose) std::printf("Band %d does not appear to have Date information in slc metadata domain \n", b + 1);
-                return FPL_ERR_DATE;
-            }
-            dates[b] = date;
-            if (!resolve_vrt_band(in, vrt, b, bands[b], 0)) {
-                if (verbose) std::printf("Cannot resolve the source of band %d\n", b + 1);
-                return FPL_ERR_OPEN_STACK;
-            }
-            if (bands[b].bytes != 8) return FPL_ERR_OPEN_STACK;
         }
-    }
 
-    // ---- output folder (evd.cpp:226-263) ----
-    const std::string outdir = opts->outputFolder;
-    struct stat st;
-    if (::stat(outdir.c_str(), &st) == 0) {
-        if (verbose) std::printf("Output folder : %s already exists \n", outdir.c_str());
-        return S_ISDIR(st.st_mode) ? FPL_ERR_OUT_EXISTS_DIR : FPL_ERR_OUT_EXISTS_FILE;
-    }
-    if (::mkdir(outdir.c_str(), 0777) != 0) return FPL_ERR_OUT_MKDIR;
-
-    // ---- outputs (evd.cpp:266-366) ----
-    std::vector<std::unique_ptr<OutFile>> slcs(nbands);
-    for (int b = 0; b < nbands; ++b) {
-        slcs[b].reset(new OutFile());
-        if (!create_output(join_path(outdir, dates[b] + ".slc"), cols, rows, 8, 6, *slcs[b]))
-            return FPL_ERR_CREATE_SLC;
-    }
-    OutFile corr, comp;
-    if (!create_output(join_path(outdir, "tcorr.bin"), cols, rows, 4, 4, corr)) return FPL_ERR_CREATE_AUX;
-    const std::string cdir = opts->outputCompressedSlcFolder ? opts->outputCompressedSlcFolder : outdir;
-    const std::string cname = opts->compSlc ? opts->compSlc : "compslc.bin";
-    if (!create_output(join_path(cdir, cname), cols, rows, 8, 6, comp)) return FPL_ERR_CREATE_AUX;
-
-    // ---- block sizes (evd.cpp:169-187) ----
-    const int blocksize = opts->blocksize > 0 ? opts->blocksize : 64;
-    int boxesperblock = int((opts->memsize * 1.0e6) / cols) / (blocksize * (nbands * 20 + 4 + nulong));
-    int blockysize = boxesperblock * blocksize;
-    if (blockysize < blocksize) blockysize = blocksize;
-    if (blockysize > rows) blockysize = rows;
-    if (verbose) std::printf("Block size = %d lines \n", blockysize);
-
-    fpl_ctx *ctx = nullptr;
-    int rc = fpl_ctx_create(opts->device, &ctx);
-    if (rc) return rc;
-    std::unique_ptr<fpl_ctx, int (*)(fpl_ctx *)> guard(ctx, fpl_ctx_destroy);
-
-    std::vector<float> stack((size_t)nbands * blockysize * cols * 2);
-    std::vector<uint32_t> nmap((size_t)blockysize * cols * nulong);
-    std::vector<float> phase((size_t)nbands * blockysize * cols * 2), tcorr((size_t)blockysize * cols),
-        compv((size_t)blockysize * cols * 2);
-
-    int yoff = 0, blockcount = 0;
-    while (yoff < rows) {
-        blockcount++;
-        int inysize = blockysize;
-        if (yoff + inysize > rows) inysize = rows - yoff;
-        int firstlinetowrite, linestowrite, rollback;       // evd.cpp:419-443
-        if (blockcount == 1) {
-            firstlinetowrite = 0;
-            linestowrite = inysize - Ny;
-            rollback = Ny;
-            if (yoff + blockysize >= rows) { linestowrite = inysize; rollback = 0; }
-        } else if (yoff + blockysize >= rows) {
-            firstlinetowrite = Ny;
-            linestowrite = inysize - Ny;
-            rollback = 0;
-        } else {
-            firstlinetowrite = Ny;
-            linestowrite = inysize - 2 * Ny;
-            rollback = 0;
+        // ---- output folder (evd.cpp:226-263) ----
+        const std::string outdir = opts->outputFolder;
+        struct stat st;
+        if (::stat(outdir.c_str(), &st) == 0) {
+            if (verbose) std::printf("Output folder : %s already exists \n", outdir.c_str());
+            return S_ISDIR(st.st_mode) ? FPL_ERR_OUT_EXISTS_DIR : FPL_ERR_OUT_EXISTS_FILE;
         }
-        const size_t plane = (size_t)inysize * cols;
-        for (int b = 0; b < nbands; ++b)
-            if (!read_rows(bands[b], cols, yoff, inysize, stack.data() + 2 * b * plane)) return FPL_ERR_READ_STACK;
-        if (!read_rows(wband[0], cols, yoff, inysize, nmap.data())) return FPL_ERR_READ_WEIGHTS;
+        if (::mkdir(outdir.c_str(), 0777) != 0) return FPL_ERR_OUT_MKDIR;
 
-        fpl_job job;
-        std::memset(&job, 0, sizeof(job));
-        job.rows = inysize;
-        job.cols = cols;
-        job.nbands = nbands;
-        job.half_window_y = Ny;
-        job.half_window_x = Nx;
-        job.method = meth;
-        job.semantics = opts->semantics;
-        job.mini_stack_count = opts->miniStackCount;
-        job.band_width = opts->bandWidth;
-        job.min_neighbors = opts->minNeighbors;
-        job.precision = opts->precision;
-        job.memory = FPL_MEM_HOST;
-        job.row_begin = firstlinetowrite;
-        job.row_end = firstlinetowrite + linestowrite;
-        job.stack = stack.data();
-        job.nmap = nmap.data();
-        job.phase = phase.data();
-        job.tcorr = tcorr.data();
-        job.comp = compv.data();
-        if (linestowrite > 0) {
-            rc = fpl_run(ctx, &job);
-            if (rc) return rc;
-            const size_t off = (size_t)firstlinetowrite * cols;
+        // ---- outputs (evd.cpp:266-366) ----
+        std::vector<std::unique_ptr<OutFile>> slcs(nbands);
+        for (int b = 0; b < nbands; ++b) {
+            slcs[b].reset(new OutFile());
+            if (!create_output(join_path(outdir, dates[b] + ".slc"), cols, rows, 8, 6, *slcs[b]))
+                return FPL_ERR_CREATE_SLC;
+        }
+        OutFile corr, comp;
+        if (!create_output(join_path(outdir, "tcorr.bin"), cols, rows, 4, 4, corr)) return FPL_ERR_CREATE_AUX;
+        const std::string cdir = opts->outputCompressedSlcFolder ? opts->outputCompressedSlcFolder : outdir;
+        const std::string cname = opts->compSlc ? opts->compSlc : "compslc.bin";
+        if (!create_output(join_path(cdir, cname), cols, rows, 8, 6, comp)) return FPL_ERR_CREATE_AUX;
+
+        // ---- block sizes (evd.cpp:169-187) ----
+        const int blocksize = opts->blocksize > 0 ? opts->blocksize : 64;
+        int boxesperblock = int((opts->memsize * 1.0e6) / cols) / (blocksize * (nbands * 20 + 4 + nulong));
+        int blockysize = boxesperblock * blocksize;
+        if (blockysize < blocksize) blockysize = blocksize;
+        if (blockysize > rows) blockysize = rows;
+        if (verbose) std::printf("Block size = %d lines \n", blockysize);
+
+        fpl_ctx *ctx = nullptr;
+        int rc = fpl_ctx_create(opts->device, &ctx);
+        if (rc) return rc;
+        std::unique_ptr<fpl_ctx, int (*)(fpl_ctx *)> guard(ctx, fpl_ctx_destroy);
+
+        std::vector<float> stack((size_t)nbands * blockysize * cols * 2);
+        std::vector<uint32_t> nmap((size_t)blockysize * cols * nulong);
+        std::vector<float> phase((size_t)nbands * blockysize * cols * 2), tcorr((size_t)blockysize * cols),
+            compv((size_t)blockysize * cols * 2);
+
+        int yoff = 0, blockcount = 0;
+        while (yoff < rows) {
+            blockcount++;
+            int inysize = blockysize;
+            if (yoff + inysize > rows) inysize = rows - yoff;
+            int firstlinetowrite, linestowrite, rollback;       // evd.cpp:419-443
+            if (blockcount == 1) {
+                firstlinetowrite = 0;
+                linestowrite = inysize - Ny;
+                rollback = Ny;
+                if (yoff + blockysize >= rows) { linestowrite = inysize; rollback = 0; }
+            } else if (yoff + blockysize >= rows) {
+                firstlinetowrite = Ny;
+                linestowrite = inysize - Ny;
+                rollback = 0;
+            } else {
+                firstlinetowrite = Ny;
+                linestowrite = inysize - 2 * Ny;
+                rollback = 0;
+            }
+            const size_t plane = (size_t)inysize * cols;
             for (int b = 0; b < nbands; ++b)
-                if (!write_rows(*slcs[b], cols, 8, yoff + firstlinetowrite, linestowrite,
-                                phase.data() + 2 * (b * plane + off)))
-                    return FPL_ERR_WRITE_SLC;
-            if (!write_rows(corr, cols, 4, yoff + firstlinetowrite, linestowrite, tcorr.data() + off))
-                return FPL_ERR_WRITE_AUX;
-            if (!write_rows(comp, cols, 8, yoff + firstlinetowrite, linestowrite, compv.data() + 2 * off))
-                return FPL_ERR_WRITE_AUX;
+                if (!read_rows(bands[b], cols, yoff, inysize, stack.data() + 2 * b * plane)) return FPL_ERR_READ_STACK;
+            if (!read_rows(wband[0], cols, yoff, inysize, nmap.data())) return FPL_ERR_READ_WEIGHTS;
+
+            fpl_job job;
+            std::memset(&job, 0, sizeof(job));
+            job.rows = inysize;
+            job.cols = cols;
+            job.nbands = nbands;
+            job.half_window_y = Ny;
+            job.half_window_x = Nx;
+            job.method = meth;
+            job.semantics = opts->semantics;
+            job.mini_stack_count = opts->miniStackCount;
+            job.band_width = opts->bandWidth;
+            job.min_neighbors = opts->minNeighbors;
+            job.precision = opts->precision;
+            job.memory = FPL_MEM_HOST;
+            job.row_begin = firstlinetowrite;
+            job.row_end = firstlinetowrite + linestowrite;
+            job.stack = stack.data();
+            job.nmap = nmap.data();
+            job.phase = phase.data();
+            job.tcorr = tcorr.data();
+            job.comp = compv.data();
+            if (linestowrite > 0) {
+                rc = fpl_run(ctx, &job);
+                if (rc) return rc;
+                const size_t off = (size_t)firstlinetowrite * cols;
+                for (int b = 0; b < nbands; ++b)
+                    if (!write_rows(*slcs[b], cols, 8, yoff + firstlinetowrite, linestowrite,
+                                    phase.data() + 2 * (b * plane + off)))
+                        return FPL_ERR_WRITE_SLC;
+                if (!write_rows(corr, cols, 4, yoff + firstlinetowrite, linestowrite, tcorr.data() + off))
+                    return FPL_ERR_WRITE_AUX;
+                if (!write_rows(comp, cols, 8, yoff + firstlinetowrite, linestowrite, compv.data() + 2 * off))
+                    return FPL_ERR_WRITE_AUX;
+            }
+            if (yoff + blockysize < rows) yoff += linestowrite - rollback;   // evd.cpp:861-868
+            else yoff = rows;
+            if (verbose) std::printf("block %d done (%d/%d lines)\n", blockcount, yoff, rows);
         }
-        if (yoff + blockysize < rows) yoff += linestowrite - rollback;   // evd.cpp:861-868
-        else yoff = rows;
-        if (verbose) std::printf("block %d done (%d/%d lines)\n", blockcount, yoff, rows);
-    }
-    return FPL_OK;
+        return FPL_OK;
+    });
 }
 
 }  // extern "C"

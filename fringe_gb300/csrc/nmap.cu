@@ -58,6 +58,7 @@
 
 #include "ctx.h"
 #include "fringe_gb300.h"
+#include "guard.h"
 
 namespace fpl {
 namespace {
@@ -517,125 +518,127 @@ int nm_tile_rows(K kern, int nb, int ny, int nx, size_t *smem)
 
 extern "C" int fpl_nmap(fpl_ctx *ctx, const fpl_nmap_job *job)
 {
-    using namespace fpl;
-    if (!ctx || !job || !job->stack || !job->nmap) return FPL_ERR_NULL;
-    if (job->rows <= 0 || job->cols <= 0 || job->nbands <= 0 || job->half_window_x < 0 ||
-        job->half_window_y < 0)
-        return FPL_ERR_OPTIONS;
-    if (job->memory != FPL_MEM_HOST && job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
-    if (!(job->prob >= 0.0) || job->prob > 1.0) return FPL_ERR_OPTIONS;
-    if (job->nbands > FPL_MAX_BANDS) return FPL_ERR_UNSUPPORTED;
-    const int wx = 2 * job->half_window_x + 1, K = (2 * job->half_window_y + 1) * wx;
-    const int nul = (K + 31) / 32;
-    if (nul > FPL_MAX_NULONG) return FPL_ERR_UNSUPPORTED;
-    NmapParams P;
-    std::memset(&P, 0, sizeof(P));
-    P.rows = job->rows;
-    P.cols = job->cols;
-    P.nb = job->nbands;
-    P.ny = job->half_window_y;
-    P.nx = job->half_window_x;
-    P.nulong = nul;
-    P.plane = (long long)job->rows * job->cols;
-    // calibration constants normalised to the first band (nmap.cpp:204-230)
-    double a[FPL_MAX_BANDS];
-    for (int b = 0; b < P.nb; ++b) {
-        const double cst = job->amp_const ? job->amp_const[b] : 1.0;
-        a[b] = cst > 0.0 ? cst : 1.0;
-    }
-    const double a0 = a[0];
-    for (int b = 0; b < P.nb; ++b) a[b] /= a0;
-    a[0] = 1.0;
-    P.unit_alpha = 1;
-    for (int b = 0; b < P.nb; ++b) {
-        P.alpha[b] = a[b];
-        if (a[b] != 1.0) P.unit_alpha = 0;
-    }
-    if (job->method != FPL_NMAP_KS2 && job->method != FPL_NMAP_AD2) return FPL_ERR_OPTIONS;
-    const bool ad2 = job->method == FPL_NMAP_AD2;
-    if (!ad2 && !ks_table(P.nb, job->prob, &P.pass_lo, &P.pass_hi)) {
-        ctx->last_error = "the threshold lies within rounding of a Kolmogorov table value for this stack depth";
-        return FPL_ERR_OPTIONS;
-    }
-    if (ad2 && !ad_table(P.nb, job->prob, &P)) {
-        ctx->last_error = "the threshold lies within rounding of the Anderson-Darling p-value for this stack depth";
-        return FPL_ERR_OPTIONS;
-    }
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return FPL_ERR_CUDA;
-    auto kern = ad2 ? k_nmap_fwd<1> : k_nmap_fwd<0>;
-    size_t smem = 0;
-    P.tr = nm_tile_rows(kern, P.nb, P.ny, P.nx, &smem);
-    if (P.tr <= 0) return FPL_ERR_UNSUPPORTED;
-    cudaStream_t st = ctx->stream;
-    const size_t b_stack = (size_t)P.plane * P.nb * 8, b_nmap = (size_t)P.plane * nul * 4;
-    const size_t b_sorted = ((size_t)P.plane * P.nb * 4 + 255) & ~size_t(255);   // keeps every region 256-aligned
-    // scratch: sorted amplitudes | validity | forward results | (host jobs)
-    // mask, stack, nmap, count
-    P.fw = ((K - (P.ny * wx + P.nx)) + 31) / 32;
-    const size_t b_fwd = ((size_t)P.plane * P.fw * 4 + 255) & ~size_t(255);
-    size_t need = b_sorted + ((P.plane + 255) & ~255ll) + b_fwd;
-    if (job->memory == FPL_MEM_HOST)
-        need += ((b_stack + 255) & ~size_t(255)) + ((b_nmap + 255) & ~size_t(255)) +
-                (((size_t)P.plane * 4 + 255) & ~size_t(255)) + (((size_t)P.plane + 255) & ~size_t(255));
-    if (ctx->cap_nm < need) {
-        if (ctx->d_nm) cudaFree(ctx->d_nm);
-        ctx->d_nm = nullptr;
-        ctx->cap_nm = 0;
-        if (cudaMalloc(&ctx->d_nm, need) != cudaSuccess) return FPL_ERR_NOMEM;
-        ctx->cap_nm = need;
-    }
-    char *base = static_cast<char *>(ctx->d_nm);
-    P.sorted = reinterpret_cast<float *>(base);
-    base += b_sorted;
-    P.valid = reinterpret_cast<uint8_t *>(base);
-    base += (P.plane + 255) & ~255ll;
-    P.fwd = reinterpret_cast<uint32_t *>(base);
-    base += b_fwd;
-    auto fail = [&](cudaError_t e, const char *what) {
-        ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
-        return FPL_ERR_CUDA;
-    };
-    cudaError_t e;
-    if (job->memory == FPL_MEM_HOST) {
-        void *d_stack = base;
-        base += (b_stack + 255) & ~size_t(255);
-        P.nmap = reinterpret_cast<uint32_t *>(base);
-        base += (b_nmap + 255) & ~size_t(255);
-        P.count = job->count ? reinterpret_cast<int32_t *>(base) : nullptr;
-        base += ((size_t)P.plane * 4 + 255) & ~size_t(255);
-        uint8_t *d_mask = job->mask ? reinterpret_cast<uint8_t *>(base) : nullptr;
-        if ((e = cudaMemcpyAsync(d_stack, job->stack, b_stack, cudaMemcpyHostToDevice, st)) != cudaSuccess)
-            return fail(e, "copy stack");
-        if (d_mask && (e = cudaMemcpyAsync(d_mask, job->mask, (size_t)P.plane, cudaMemcpyHostToDevice, st)) !=
-                          cudaSuccess)
-            return fail(e, "copy mask");
-        P.stack = static_cast<const float2 *>(d_stack);
-        P.mask = d_mask;
-    } else {
-        P.stack = static_cast<const float2 *>(job->stack);
-        P.mask = job->mask;
-        P.nmap = job->nmap;
-        P.count = job->count;
-    }
-    const unsigned sblocks = (unsigned)((P.plane + 127) / 128);
-    if (P.nb <= 16) k_nmap_sort<16><<<sblocks, 128, 0, st>>>(P);
-    else if (P.nb <= 32) k_nmap_sort<32><<<sblocks, 128, 0, st>>>(P);
-    else k_nmap_sort<64><<<sblocks, 128, 0, st>>>(P);
-    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_sort");
-    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
-        return fail(e, "k_nmap_fwd attributes");
-    const long long ntiles = (long long)((P.cols + NM_TC - 1) / NM_TC) * ((P.rows + P.tr - 1) / P.tr);
-    kern<<<(unsigned)ntiles, NM_TC * P.tr, smem, st>>>(P);
-    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_fwd");
-    k_nmap_mirror<<<(unsigned)((P.plane + 255) / 256), 256, 0, st>>>(P);
-    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_mirror");
-    if (job->memory == FPL_MEM_HOST) {
-        if ((e = cudaMemcpyAsync(job->nmap, P.nmap, b_nmap, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-            return fail(e, "copy nmap");
-        if (job->count &&
-            (e = cudaMemcpyAsync(job->count, P.count, (size_t)P.plane * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-            return fail(e, "copy count");
-    }
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail(e, "fpl_nmap");
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        using namespace fpl;
+        if (!ctx || !job || !job->stack || !job->nmap) return FPL_ERR_NULL;
+        if (job->rows <= 0 || job->cols <= 0 || job->nbands <= 0 || job->half_window_x < 0 ||
+            job->half_window_y < 0)
+            return FPL_ERR_OPTIONS;
+        if (job->memory != FPL_MEM_HOST && job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
+        if (!(job->prob >= 0.0) || job->prob > 1.0) return FPL_ERR_OPTIONS;
+        if (job->nbands > FPL_MAX_BANDS) return FPL_ERR_UNSUPPORTED;
+        const int wx = 2 * job->half_window_x + 1, K = (2 * job->half_window_y + 1) * wx;
+        const int nul = (K + 31) / 32;
+        if (nul > FPL_MAX_NULONG) return FPL_ERR_UNSUPPORTED;
+        NmapParams P;
+        std::memset(&P, 0, sizeof(P));
+        P.rows = job->rows;
+        P.cols = job->cols;
+        P.nb = job->nbands;
+        P.ny = job->half_window_y;
+        P.nx = job->half_window_x;
+        P.nulong = nul;
+        P.plane = (long long)job->rows * job->cols;
+        // calibration constants normalised to the first band (nmap.cpp:204-230)
+        double a[FPL_MAX_BANDS];
+        for (int b = 0; b < P.nb; ++b) {
+            const double cst = job->amp_const ? job->amp_const[b] : 1.0;
+            a[b] = cst > 0.0 ? cst : 1.0;
+        }
+        const double a0 = a[0];
+        for (int b = 0; b < P.nb; ++b) a[b] /= a0;
+        a[0] = 1.0;
+        P.unit_alpha = 1;
+        for (int b = 0; b < P.nb; ++b) {
+            P.alpha[b] = a[b];
+            if (a[b] != 1.0) P.unit_alpha = 0;
+        }
+        if (job->method != FPL_NMAP_KS2 && job->method != FPL_NMAP_AD2) return FPL_ERR_OPTIONS;
+        const bool ad2 = job->method == FPL_NMAP_AD2;
+        if (!ad2 && !ks_table(P.nb, job->prob, &P.pass_lo, &P.pass_hi)) {
+            ctx->last_error = "the threshold lies within rounding of a Kolmogorov table value for this stack depth";
+            return FPL_ERR_OPTIONS;
+        }
+        if (ad2 && !ad_table(P.nb, job->prob, &P)) {
+            ctx->last_error = "the threshold lies within rounding of the Anderson-Darling p-value for this stack depth";
+            return FPL_ERR_OPTIONS;
+        }
+        if (cudaSetDevice(ctx->device) != cudaSuccess) return FPL_ERR_CUDA;
+        auto kern = ad2 ? k_nmap_fwd<1> : k_nmap_fwd<0>;
+        size_t smem = 0;
+        P.tr = nm_tile_rows(kern, P.nb, P.ny, P.nx, &smem);
+        if (P.tr <= 0) return FPL_ERR_UNSUPPORTED;
+        cudaStream_t st = ctx->stream;
+        const size_t b_stack = (size_t)P.plane * P.nb * 8, b_nmap = (size_t)P.plane * nul * 4;
+        const size_t b_sorted = ((size_t)P.plane * P.nb * 4 + 255) & ~size_t(255);   // keeps every region 256-aligned
+        // scratch: sorted amplitudes | validity | forward results | (host jobs)
+        // mask, stack, nmap, count
+        P.fw = ((K - (P.ny * wx + P.nx)) + 31) / 32;
+        const size_t b_fwd = ((size_t)P.plane * P.fw * 4 + 255) & ~size_t(255);
+        size_t need = b_sorted + ((P.plane + 255) & ~255ll) + b_fwd;
+        if (job->memory == FPL_MEM_HOST)
+            need += ((b_stack + 255) & ~size_t(255)) + ((b_nmap + 255) & ~size_t(255)) +
+                    (((size_t)P.plane * 4 + 255) & ~size_t(255)) + (((size_t)P.plane + 255) & ~size_t(255));
+        if (ctx->cap_nm < need) {
+            if (ctx->d_nm) cudaFree(ctx->d_nm);
+            ctx->d_nm = nullptr;
+            ctx->cap_nm = 0;
+            if (cudaMalloc(&ctx->d_nm, need) != cudaSuccess) return FPL_ERR_NOMEM;
+            ctx->cap_nm = need;
+        }
+        char *base = static_cast<char *>(ctx->d_nm);
+        P.sorted = reinterpret_cast<float *>(base);
+        base += b_sorted;
+        P.valid = reinterpret_cast<uint8_t *>(base);
+        base += (P.plane + 255) & ~255ll;
+        P.fwd = reinterpret_cast<uint32_t *>(base);
+        base += b_fwd;
+        auto fail = [&](cudaError_t e, const char *what) {
+            ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+            return FPL_ERR_CUDA;
+        };
+        cudaError_t e;
+        if (job->memory == FPL_MEM_HOST) {
+            void *d_stack = base;
+            base += (b_stack + 255) & ~size_t(255);
+            P.nmap = reinterpret_cast<uint32_t *>(base);
+            base += (b_nmap + 255) & ~size_t(255);
+            P.count = job->count ? reinterpret_cast<int32_t *>(base) : nullptr;
+            base += ((size_t)P.plane * 4 + 255) & ~size_t(255);
+            uint8_t *d_mask = job->mask ? reinterpret_cast<uint8_t *>(base) : nullptr;
+            if ((e = cudaMemcpyAsync(d_stack, job->stack, b_stack, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+                return fail(e, "copy stack");
+            if (d_mask && (e = cudaMemcpyAsync(d_mask, job->mask, (size_t)P.plane, cudaMemcpyHostToDevice, st)) !=
+                              cudaSuccess)
+                return fail(e, "copy mask");
+            P.stack = static_cast<const float2 *>(d_stack);
+            P.mask = d_mask;
+        } else {
+            P.stack = static_cast<const float2 *>(job->stack);
+            P.mask = job->mask;
+            P.nmap = job->nmap;
+            P.count = job->count;
+        }
+        const unsigned sblocks = (unsigned)((P.plane + 127) / 128);
+        if (P.nb <= 16) k_nmap_sort<16><<<sblocks, 128, 0, st>>>(P);
+        else if (P.nb <= 32) k_nmap_sort<32><<<sblocks, 128, 0, st>>>(P);
+        else k_nmap_sort<64><<<sblocks, 128, 0, st>>>(P);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_sort");
+        if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+            return fail(e, "k_nmap_fwd attributes");
+        const long long ntiles = (long long)((P.cols + NM_TC - 1) / NM_TC) * ((P.rows + P.tr - 1) / P.tr);
+        kern<<<(unsigned)ntiles, NM_TC * P.tr, smem, st>>>(P);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_fwd");
+        k_nmap_mirror<<<(unsigned)((P.plane + 255) / 256), 256, 0, st>>>(P);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "k_nmap_mirror");
+        if (job->memory == FPL_MEM_HOST) {
+            if ((e = cudaMemcpyAsync(job->nmap, P.nmap, b_nmap, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+                return fail(e, "copy nmap");
+            if (job->count &&
+                (e = cudaMemcpyAsync(job->count, P.count, (size_t)P.plane * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+                return fail(e, "copy count");
+        }
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail(e, "fpl_nmap");
+        return FPL_OK;
+    });
 }

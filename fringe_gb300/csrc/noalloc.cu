@@ -30,6 +30,7 @@
 
 #include "ctx.h"
 #include "fringe_gb300.h"
+#include "guard.h"
 #include "kernels.h"
 #include "pixel.cuh"
 
@@ -73,57 +74,59 @@ int noalloc_setup(int dev, unsigned char **addr, int *sms)
 
 extern "C" int fpl_run_noalloc(const fpl_job *job, void *stream)
 {
-    int rc = fpl_validate_job(job);
-    if (rc) return rc;
-    if (job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
-    const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
-    const long long npix = (long long)(r1 - r0) * job->cols;
-    if (npix > FPL_NOALLOC_MAX_PIXELS) return FPL_ERR_NOALLOC_LIMIT;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return FPL_ERR_CUDA;
-    unsigned char *scratch = nullptr;
-    int sms = 0;
-    rc = noalloc_setup(dev, &scratch, &sms);
-    if (rc) return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return fpl_guard([&]() -> int {
+        int rc = fpl_validate_job(job);
+        if (rc) return rc;
+        if (job->memory != FPL_MEM_DEVICE) return FPL_ERR_OPTIONS;
+        const int r0 = job->row_begin, r1 = job->row_end <= 0 ? job->rows : job->row_end;
+        const long long npix = (long long)(r1 - r0) * job->cols;
+        if (npix > FPL_NOALLOC_MAX_PIXELS) return FPL_ERR_NOALLOC_LIMIT;
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return FPL_ERR_CUDA;
+        unsigned char *scratch = nullptr;
+        int sms = 0;
+        rc = noalloc_setup(dev, &scratch, &sms);
+        if (rc) return rc;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
 
-    fpl::KParams P;
-    std::memset(&P, 0, sizeof(P));
-    P.stack = static_cast<const float2 *>(job->stack);
-    P.nmap = job->nmap;
-    P.phase = static_cast<float2 *>(job->phase);
-    P.tcorr = job->tcorr;
-    P.comp = static_cast<float2 *>(job->comp);
-    P.status = job->status;
-    P.rows = job->rows;
-    P.cols = job->cols;
-    P.nb = job->nbands;
-    P.ny = job->half_window_y;
-    P.nx = job->half_window_x;
-    P.wx = 2 * job->half_window_x + 1;
-    P.K = (2 * job->half_window_y + 1) * P.wx;
-    P.nulong = (P.K + 31) / 32;
-    P.plane = (long long)job->rows * job->cols;
-    P.pix_begin = (long long)r0 * job->cols;
-    P.npix = npix;
-    P.method = job->method;
-    P.semantics = job->semantics;
-    P.mini = job->mini_stack_count;
-    P.bw = job->band_width;
-    P.min_neigh = job->min_neighbors;
-    P.amb = kDefaultAmbScale;
-    P.cond_max = kDefaultCondMax;
-    P.shift = kDefaultShift;
-    P.shift_backoff = kDefaultShiftBackoff;
-    P.fb_count = reinterpret_cast<int *>(scratch);
-    P.err = reinterpret_cast<unsigned *>(scratch + 16);
-    P.slow = reinterpret_cast<int *>(scratch + 32);
-    P.fb_list = reinterpret_cast<long long *>(scratch + kCounterBytes);
-    P.fb_cap = FPL_NOALLOC_MAX_PIXELS;
-    // the counters must start at zero; the list itself is written before it is read
-    if (cudaMemsetAsync(scratch, 0, 64, st) != cudaSuccess) return FPL_ERR_CUDA;
-    if (npix == 0) return FPL_OK;
-    if (fpl::launch_fp32(P, sms, st) != cudaSuccess) return FPL_ERR_CUDA;
-    if (fpl::launch_fp64(P, sms, st) != cudaSuccess) return FPL_ERR_CUDA;
-    return FPL_OK;
+        fpl::KParams P;
+        std::memset(&P, 0, sizeof(P));
+        P.stack = static_cast<const float2 *>(job->stack);
+        P.nmap = job->nmap;
+        P.phase = static_cast<float2 *>(job->phase);
+        P.tcorr = job->tcorr;
+        P.comp = static_cast<float2 *>(job->comp);
+        P.status = job->status;
+        P.rows = job->rows;
+        P.cols = job->cols;
+        P.nb = job->nbands;
+        P.ny = job->half_window_y;
+        P.nx = job->half_window_x;
+        P.wx = 2 * job->half_window_x + 1;
+        P.K = (2 * job->half_window_y + 1) * P.wx;
+        P.nulong = (P.K + 31) / 32;
+        P.plane = (long long)job->rows * job->cols;
+        P.pix_begin = (long long)r0 * job->cols;
+        P.npix = npix;
+        P.method = job->method;
+        P.semantics = job->semantics;
+        P.mini = job->mini_stack_count;
+        P.bw = job->band_width;
+        P.min_neigh = job->min_neighbors;
+        P.amb = kDefaultAmbScale;
+        P.cond_max = kDefaultCondMax;
+        P.shift = kDefaultShift;
+        P.shift_backoff = kDefaultShiftBackoff;
+        P.fb_count = reinterpret_cast<int *>(scratch);
+        P.err = reinterpret_cast<unsigned *>(scratch + 16);
+        P.slow = reinterpret_cast<int *>(scratch + 32);
+        P.fb_list = reinterpret_cast<long long *>(scratch + kCounterBytes);
+        P.fb_cap = FPL_NOALLOC_MAX_PIXELS;
+        // the counters must start at zero; the list itself is written before it is read
+        if (cudaMemsetAsync(scratch, 0, 64, st) != cudaSuccess) return FPL_ERR_CUDA;
+        if (npix == 0) return FPL_OK;
+        if (fpl::launch_fp32(P, sms, st) != cudaSuccess) return FPL_ERR_CUDA;
+        if (fpl::launch_fp64(P, sms, st) != cudaSuccess) return FPL_ERR_CUDA;
+        return FPL_OK;
+    });
 }

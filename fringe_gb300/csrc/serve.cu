@@ -33,6 +33,7 @@
 #include "batch.h"
 #include "ctx.h"
 #include "fringe_gb300.h"
+#include "guard.h"
 #include "kernels.h"
 
 namespace {
@@ -412,120 +413,128 @@ void fpl_server_config_default(fpl_server_config *c)
 
 int fpl_server_create(const fpl_server_config *cfg, fpl_server **out)
 {
-    if (!cfg || !out) return FPL_ERR_NULL;
-    *out = nullptr;
-    if (cfg->wave_pixels <= 0 || cfg->memory_budget == 0) return FPL_ERR_OPTIONS;
-    if (cudaSetDevice(cfg->device) != cudaSuccess) return FPL_ERR_CUDA;
-    fpl_server *s = new fpl_server();
-    s->cfg = *cfg;
-    cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
-    bool ok = cudaStreamCreateWithFlags(&s->s_copy, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&s->s_compute, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaEventCreateWithFlags(&s->ev_wave, cudaEventDisableTiming) == cudaSuccess &&
-              cudaMalloc(&s->d_table, sizeof(fpl::BatchEntry) * s->max_pieces) == cudaSuccess &&
-              cudaMallocHost(&s->h_table, sizeof(fpl::BatchEntry) * s->max_pieces) == cudaSuccess &&
-              cudaMalloc(&s->d_segs, sizeof(fpl::BoxSeg) * s->max_pieces) == cudaSuccess &&
-              cudaMallocHost(&s->h_segs, sizeof(fpl::BoxSeg) * s->max_pieces) == cudaSuccess;
-    // counters | work counters | work lists (a wave holds at most wave_pixels
-    // plus one row per job beyond its share)
-    s->wave_bytes = kPieceCounterBytes * s->max_pieces + 64 +
-                    sizeof(long long) * (size_t)(cfg->wave_pixels + (long long)s->max_pieces * 65536);
-    ok = ok && cudaMalloc(&s->d_wave, s->wave_bytes) == cudaSuccess;
-    if (!ok) {
-        s->stop = true;
-        fpl_server_destroy(s);
-        return FPL_ERR_NOMEM;
-    }
-    s->th = std::thread(scheduler, s);
-    *out = s;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!cfg || !out) return FPL_ERR_NULL;
+        *out = nullptr;
+        if (cfg->wave_pixels <= 0 || cfg->memory_budget == 0) return FPL_ERR_OPTIONS;
+        if (cudaSetDevice(cfg->device) != cudaSuccess) return FPL_ERR_CUDA;
+        fpl_server *s = new fpl_server();
+        s->cfg = *cfg;
+        cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
+        bool ok = cudaStreamCreateWithFlags(&s->s_copy, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&s->s_compute, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&s->ev_wave, cudaEventDisableTiming) == cudaSuccess &&
+                  cudaMalloc(&s->d_table, sizeof(fpl::BatchEntry) * s->max_pieces) == cudaSuccess &&
+                  cudaMallocHost(&s->h_table, sizeof(fpl::BatchEntry) * s->max_pieces) == cudaSuccess &&
+                  cudaMalloc(&s->d_segs, sizeof(fpl::BoxSeg) * s->max_pieces) == cudaSuccess &&
+                  cudaMallocHost(&s->h_segs, sizeof(fpl::BoxSeg) * s->max_pieces) == cudaSuccess;
+        // counters | work counters | work lists (a wave holds at most wave_pixels
+        // plus one row per job beyond its share)
+        s->wave_bytes = kPieceCounterBytes * s->max_pieces + 64 +
+                        sizeof(long long) * (size_t)(cfg->wave_pixels + (long long)s->max_pieces * 65536);
+        ok = ok && cudaMalloc(&s->d_wave, s->wave_bytes) == cudaSuccess;
+        if (!ok) {
+            s->stop = true;
+            fpl_server_destroy(s);
+            return FPL_ERR_NOMEM;
+        }
+        s->th = std::thread(scheduler, s);
+        *out = s;
+        return FPL_OK;
+    });
 }
 
 int fpl_server_submit(fpl_server *s, const fpl_job *job, unsigned long long *ticket)
 {
-    if (!s || !ticket) return FPL_ERR_NULL;
-    int rc = fpl_validate_job(job);
-    if (rc) return rc;
-    if (job->memory != FPL_MEM_HOST) return FPL_ERR_OPTIONS;
-    if (job->cols > 65536) return FPL_ERR_UNSUPPORTED;   // a row must fit the wave's work list slack
-    SJob *j = new SJob();
-    j->host = *job;
-    j->bytes = footprint(*job);
-    j->r0 = job->row_begin;
-    j->r1 = job->row_end <= 0 ? job->rows : job->row_end;
-    j->next_row = j->r0;
-    j->t_submit = clk::now();
-    if (cudaEventCreateWithFlags(&j->ev_in, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&j->ev_out, cudaEventDisableTiming) != cudaSuccess) {
-        delete j;
-        return FPL_ERR_CUDA;
-    }
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->fatal) {
-        delete j;
-        return s->fatal;
-    }
-    j->ticket = s->next_ticket++;
-    s->jobs[j->ticket] = j;
-    s->pending.push_back(j);
-    *ticket = j->ticket;
-    s->cv.notify_all();
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!s || !ticket) return FPL_ERR_NULL;
+        int rc = fpl_validate_job(job);
+        if (rc) return rc;
+        if (job->memory != FPL_MEM_HOST) return FPL_ERR_OPTIONS;
+        if (job->cols > 65536) return FPL_ERR_UNSUPPORTED;   // a row must fit the wave's work list slack
+        SJob *j = new SJob();
+        j->host = *job;
+        j->bytes = footprint(*job);
+        j->r0 = job->row_begin;
+        j->r1 = job->row_end <= 0 ? job->rows : job->row_end;
+        j->next_row = j->r0;
+        j->t_submit = clk::now();
+        if (cudaEventCreateWithFlags(&j->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&j->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+            delete j;
+            return FPL_ERR_CUDA;
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->fatal) {
+            delete j;
+            return s->fatal;
+        }
+        j->ticket = s->next_ticket++;
+        s->jobs[j->ticket] = j;
+        s->pending.push_back(j);
+        *ticket = j->ticket;
+        s->cv.notify_all();
+        return FPL_OK;
+    });
 }
 
 int fpl_server_wait(fpl_server *s, unsigned long long ticket, double timeout_s, fpl_ticket_info *info)
 {
-    if (!s) return FPL_ERR_NULL;
-    std::unique_lock<std::mutex> lk(s->mu);
-    auto it = s->jobs.find(ticket);
-    if (it == s->jobs.end()) return FPL_ERR_OPTIONS;
-    SJob *j = it->second;
-    const auto deadline = clk::now() + std::chrono::duration<double>(timeout_s);
-    while (j->state != DONE && j->state != FAILED) {
-        if (s->cv.wait_until(lk, deadline) == std::cv_status::timeout &&
-            j->state != DONE && j->state != FAILED)
-            return FPL_ERR_TIMEOUT;
-    }
-    if (info) {
-        info->queue_ms = j->state == DONE ? ms_since(j->t_submit, j->t_admit) : 0.0;
-        info->run_ms = j->state == DONE ? ms_since(j->t_admit, j->t_done) : 0.0;
-        info->total_ms = j->state == DONE ? ms_since(j->t_submit, j->t_done) : 0.0;
-        info->rc = j->rc;
-    }
-    const int rc = j->state == DONE ? FPL_OK : (j->rc ? j->rc : FPL_ERR_CUDA);
-    cudaEventDestroy(j->ev_in);
-    cudaEventDestroy(j->ev_out);
-    s->jobs.erase(it);
-    delete j;
-    return rc;
+    return fpl_guard([&]() -> int {
+        if (!s) return FPL_ERR_NULL;
+        std::unique_lock<std::mutex> lk(s->mu);
+        auto it = s->jobs.find(ticket);
+        if (it == s->jobs.end()) return FPL_ERR_OPTIONS;
+        SJob *j = it->second;
+        const auto deadline = clk::now() + std::chrono::duration<double>(timeout_s);
+        while (j->state != DONE && j->state != FAILED) {
+            if (s->cv.wait_until(lk, deadline) == std::cv_status::timeout &&
+                j->state != DONE && j->state != FAILED)
+                return FPL_ERR_TIMEOUT;
+        }
+        if (info) {
+            info->queue_ms = j->state == DONE ? ms_since(j->t_submit, j->t_admit) : 0.0;
+            info->run_ms = j->state == DONE ? ms_since(j->t_admit, j->t_done) : 0.0;
+            info->total_ms = j->state == DONE ? ms_since(j->t_submit, j->t_done) : 0.0;
+            info->rc = j->rc;
+        }
+        const int rc = j->state == DONE ? FPL_OK : (j->rc ? j->rc : FPL_ERR_CUDA);
+        cudaEventDestroy(j->ev_in);
+        cudaEventDestroy(j->ev_out);
+        s->jobs.erase(it);
+        delete j;
+        return rc;
+    });
 }
 
 int fpl_server_destroy(fpl_server *s)
 {
-    if (!s) return FPL_OK;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        s->stop = true;
-        s->cv.notify_all();
-    }
-    if (s->th.joinable()) s->th.join();
-    cudaSetDevice(s->cfg.device);
-    for (auto &kv : s->jobs) {
-        if (kv.second->ev_in) cudaEventDestroy(kv.second->ev_in);
-        if (kv.second->ev_out) cudaEventDestroy(kv.second->ev_out);
-        delete kv.second;
-    }
-    if (s->d_wave) cudaFree(s->d_wave);
-    if (s->d_table) cudaFree(s->d_table);
-    if (s->h_table) cudaFreeHost(s->h_table);
-    if (s->d_segs) cudaFree(s->d_segs);
-    if (s->h_segs) cudaFreeHost(s->h_segs);
-    if (s->d_rec) cudaFree(s->d_rec);
-    if (s->ev_wave) cudaEventDestroy(s->ev_wave);
-    if (s->s_copy) cudaStreamDestroy(s->s_copy);
-    if (s->s_compute) cudaStreamDestroy(s->s_compute);
-    delete s;
-    return FPL_OK;
+    return fpl_guard([&]() -> int {
+        if (!s) return FPL_OK;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stop = true;
+            s->cv.notify_all();
+        }
+        if (s->th.joinable()) s->th.join();
+        cudaSetDevice(s->cfg.device);
+        for (auto &kv : s->jobs) {
+            if (kv.second->ev_in) cudaEventDestroy(kv.second->ev_in);
+            if (kv.second->ev_out) cudaEventDestroy(kv.second->ev_out);
+            delete kv.second;
+        }
+        if (s->d_wave) cudaFree(s->d_wave);
+        if (s->d_table) cudaFree(s->d_table);
+        if (s->h_table) cudaFreeHost(s->h_table);
+        if (s->d_segs) cudaFree(s->d_segs);
+        if (s->h_segs) cudaFreeHost(s->h_segs);
+        if (s->d_rec) cudaFree(s->d_rec);
+        if (s->ev_wave) cudaEventDestroy(s->ev_wave);
+        if (s->s_copy) cudaStreamDestroy(s->s_copy);
+        if (s->s_compute) cudaStreamDestroy(s->s_compute);
+        delete s;
+        return FPL_OK;
+    });
 }
 
 }  // extern "C"

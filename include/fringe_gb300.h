@@ -88,6 +88,7 @@ enum fpl_pixel_status {
 #define FPL_ERR_NULL           205   /* a required pointer is NULL */
 #define FPL_ERR_NOALLOC_LIMIT  206   /* job larger than fpl_run_noalloc's scratch */
 #define FPL_ERR_TIMEOUT        207   /* fpl_server_wait gave up */
+#define FPL_ERR_HOST           208   /* host-side failure (host memory, threads) */
 
 #define FPL_MAX_BANDS 64
 #define FPL_MAX_NULONG 32

@@ -55,6 +55,11 @@ def test_error_strings_and_defaults(lib):
     from fringe_gb300 import _lib
     assert lib.fpl_error_string(0) == b"ok"
     assert b"options" in lib.fpl_error_string(101)
+    # every status code the header defines has its own message
+    codes = {k: v for k, v in _lib.header_defines().items() if k == "FPL_OK" or k.startswith("FPL_ERR_")}
+    assert codes["FPL_ERR_HOST"] == 208
+    for name, code in codes.items():
+        assert lib.fpl_error_string(code) != b"unknown error", name
     o = _lib.FplOptions()
     lib.fpl_options_default(ctypes.byref(o))
     # evdOptions defaults, src/evd/evd.hpp:58-68
