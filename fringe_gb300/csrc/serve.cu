@@ -305,7 +305,7 @@ bool run_wave(fpl_server *s, std::vector<Piece> &pieces)
     return cudaEventRecord(s->ev_wave, s->s_compute) == cudaSuccess;
 }
 
-void scheduler(fpl_server *s)
+void scheduler_loop(fpl_server *s)
 {
     cudaSetDevice(s->cfg.device);
     std::vector<Piece> pieces;
@@ -396,6 +396,21 @@ void scheduler(fpl_server *s)
         }
     }
     cudaStreamSynchronize(s->s_copy);
+}
+
+// the scheduler thread: an exception (a host allocation that failed while
+// admitting jobs or building a wave) must not end the process, so it fails
+// every job with FPL_ERR_HOST, which later submissions also receive, and
+// the thread ends
+void scheduler(fpl_server *s)
+{
+    try {
+        scheduler_loop(s);
+    } catch (...) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        fail_all(s, FPL_ERR_HOST);
+        s->cv.notify_all();
+    }
 }
 
 }  // namespace
@@ -499,6 +514,13 @@ int fpl_server_wait(fpl_server *s, unsigned long long ticket, double timeout_s, 
             info->rc = j->rc;
         }
         const int rc = j->state == DONE ? FPL_OK : (j->rc ? j->rc : FPL_ERR_CUDA);
+        if (j->dmem) {
+            // a job that failed while it held device memory (a finished job
+            // has returned it): release it once the server's streams are idle
+            cudaStreamSynchronize(s->s_compute);
+            cudaStreamSynchronize(s->s_copy);
+            cudaFree(j->dmem);
+        }
         cudaEventDestroy(j->ev_in);
         cudaEventDestroy(j->ev_out);
         s->jobs.erase(it);
@@ -518,9 +540,13 @@ int fpl_server_destroy(fpl_server *s)
         }
         if (s->th.joinable()) s->th.join();
         cudaSetDevice(s->cfg.device);
+        // nothing of the server's may still run when its memory is freed
+        if (s->s_compute) cudaStreamSynchronize(s->s_compute);
+        if (s->s_copy) cudaStreamSynchronize(s->s_copy);
         for (auto &kv : s->jobs) {
             if (kv.second->ev_in) cudaEventDestroy(kv.second->ev_in);
             if (kv.second->ev_out) cudaEventDestroy(kv.second->ev_out);
+            if (kv.second->dmem) cudaFree(kv.second->dmem);     // a job failed while it held memory
             delete kv.second;
         }
         if (s->d_wave) cudaFree(s->d_wave);
