@@ -453,7 +453,13 @@ int fpl_server_create(const fpl_server_config *cfg, fpl_server **out)
             fpl_server_destroy(s);
             return FPL_ERR_NOMEM;
         }
-        s->th = std::thread(scheduler, s);
+        try {
+            s->th = std::thread(scheduler, s);
+        } catch (...) {
+            s->stop = true;
+            fpl_server_destroy(s);       // no scheduler thread to join
+            return FPL_ERR_HOST;
+        }
         *out = s;
         return FPL_OK;
     });
