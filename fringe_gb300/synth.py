@@ -147,8 +147,9 @@ def simulate_stack(rows: int, cols: int, nbands: int, seed: int, *,
 
 
 def indefinite_abs_coherence(nbands: int, rng: np.random.Generator,
-                              below: float = -0.3, tries: int = 20000) -> np.ndarray:
-    """A coherence matrix C0 = V V^H + 0.02 I (V complex, nbands x 2) scaled
+                              below: float = -0.3, tries: int = 20000,
+                              ridge: float = 0.02) -> np.ndarray:
+    """A coherence matrix C0 = V V^H + ridge I (V complex, nbands x 2) scaled
     to a unit diagonal, drawn until its magnitude |C0| has an eigenvalue
     below `below`.  C0 is positive definite; the sample coherence of a
     window of its draws keeps an indefinite magnitude (the reference's code
@@ -158,7 +159,7 @@ def indefinite_abs_coherence(nbands: int, rng: np.random.Generator,
     `tries` draws."""
     for _ in range(tries):
         V = rng.standard_normal((nbands, 2)) + 1j * rng.standard_normal((nbands, 2))
-        C0 = V @ V.conj().T + 0.02 * np.eye(nbands)
+        C0 = V @ V.conj().T + ridge * np.eye(nbands)
         d = np.sqrt(np.real(np.diag(C0)))
         C0 = C0 / np.outer(d, d)
         if np.linalg.eigvalsh(np.abs(C0))[0] < below:
@@ -177,14 +178,19 @@ def scene(kind: str, rows: int, cols: int, nbands: int, ny: int, nx: int,
                         gamma_inf = 0 (else 0.2), Voronoi nmap.
     kind = "indefabs" : every pixel drawn from one positive definite
                         coherence whose magnitude matrix is indefinite (see
-                        indefinite_abs_coherence), nmap all ones.
+                        indefinite_abs_coherence; ridge 0.02 up to 32 dates,
+                        0.5 above, which keeps lambda_min(C) of a window's
+                        sample coherence near 0.016 at 64 dates, clear of
+                        the FP32 rounding band of the 1e-6 test), nmap all
+                        ones.
     """
     rng = np.random.Generator(np.random.PCG64(seed + 7919))
     if kind == "uniform":
         st = simulate_stack(rows, cols, nbands, seed)
         return st, nmap_all_ones(rows, cols, ny, nx)
     if kind == "indefabs":
-        L = np.linalg.cholesky(indefinite_abs_coherence(nbands, rng))
+        ridge = 0.02 if nbands <= 32 else 0.5
+        L = np.linalg.cholesky(indefinite_abs_coherence(nbands, rng, ridge=ridge))
         z = (rng.standard_normal((nbands, rows * cols))
              + 1j * rng.standard_normal((nbands, rows * cols))) / np.sqrt(2.0)
         st = (L @ z).reshape(nbands, rows, cols).astype(np.complex64)
